@@ -1,0 +1,103 @@
+"""ctypes binding of ``libbsj.so`` (include/bsj.h).
+
+The library is the only compute path: if it is missing or cannot be loaded, every call
+raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libbsj.so")
+
+BSJ_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "size outside the supported limits",
+                3: "CUDA error", 4: "out of memory", 5: "device-side consistency check failed"}
+MODES = {"v1": 0, "v2": 1, "clean": 2, "ich": 3, "pms": 4}
+NO_BOUND = 500000
+MAX_JOBS, MAX_MACHINES, MAX_OPS, MAX_BEAM = 128, 64, 8192, 16384
+
+# Every symbol include/bsj.h declares (checked by the CPU tests without calling them).
+EXPORTED = [
+    "bsj_version", "bsj_status_string", "bsj_create", "bsj_destroy", "bsj_last_error",
+    "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations", "bsj_plan_create", "bsj_plan_run",
+    "bsj_plan_results", "bsj_plan_destroy", "bsj_plan_launches", "bsj_plan_stats",
+    "bsj_plan_set_timing", "bsj_plan_kernel_ms",
+]
+
+
+class BsjError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Instance(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("m", ctypes.c_int32),
+                ("machine", ctypes.POINTER(ctypes.c_int32)),
+                ("duration", ctypes.POINTER(ctypes.c_int32))]
+
+
+class Beam(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("beam_width", ctypes.c_int32),
+                ("best_known", ctypes.c_int32), ("seed", ctypes.c_uint32),
+                ("instance", ctypes.c_int32), ("bound_group", ctypes.c_int32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("makespan", ctypes.c_int32), ("found", ctypes.c_int32),
+                ("sequence", ctypes.POINTER(ctypes.c_int32)),
+                ("expanded", ctypes.c_int64), ("slots", ctypes.c_int64),
+                ("levels", ctypes.c_int32), ("group_best", ctypes.c_int32)]
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(path: Optional[str] = None) -> ctypes.CDLL:
+    """Load libbsj.so (raising if it is absent: build it with
+    ``python -c 'import __graft_entry__ as g; g.build()'``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"libbsj.so not built ({p}); run beamsearch_jssp_gpu_gb300/build.py")
+    L = ctypes.CDLL(p)
+    vp = ctypes.c_void_p
+    P = ctypes.POINTER
+    L.bsj_version.restype = ctypes.c_char_p
+    L.bsj_status_string.restype = ctypes.c_char_p
+    L.bsj_status_string.argtypes = [ctypes.c_int]
+    L.bsj_create.argtypes = [P(vp), ctypes.c_int]
+    L.bsj_destroy.argtypes = [vp]
+    L.bsj_destroy.restype = None
+    L.bsj_last_error.argtypes = [vp]
+    L.bsj_last_error.restype = ctypes.c_char_p
+    L.bsj_solve.argtypes = [vp, P(Instance), P(Beam), P(Result), vp]
+    L.bsj_solve_batch.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam), P(Result), vp]
+    L.bsj_solve_iterations.argtypes = [vp, P(Instance), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, P(ctypes.c_uint32), ctypes.c_int32,
+                                       P(ctypes.c_int32), P(ctypes.c_int32), vp]
+    L.bsj_plan_create.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam), P(vp)]
+    L.bsj_plan_run.argtypes = [vp, vp]
+    L.bsj_plan_results.argtypes = [vp, P(Result)]
+    L.bsj_plan_destroy.argtypes = [vp]
+    L.bsj_plan_destroy.restype = None
+    L.bsj_plan_launches.argtypes = [vp]
+    L.bsj_plan_launches.restype = ctypes.c_int64
+    L.bsj_plan_stats.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_int64)]
+    L.bsj_plan_set_timing.argtypes = [vp, ctypes.c_int]
+    L.bsj_plan_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int64), ctypes.c_int]
+    for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
+                 "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
+                 "bsj_plan_set_timing", "bsj_plan_kernel_ms"):
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L

@@ -1,0 +1,679 @@
+// bsj_engine.cu -- host engine and the C ABI (include/bsj.h).
+//
+// A plan is a set of beams (independent seeds and/or instances of uneven size, any mix
+// of modes) laid out in one device arena.  Running a plan enqueues every search level:
+//
+//   k_step(-1)                                   roots + level-0 expansion
+//   for s = 0 .. maxN-1:
+//       k_select(s) / k_heap(s)                  top-K per beam (gpu modes / ICH, PMS)
+//       k_gather_v1(s)                           v1 beams only
+//       k_step(s)            (s < maxN-1)        materialise level s+1, expand it
+//   k_finalize                                   makespans + schedules
+//
+// replacing the reference's per-call host loop of three launches per level with device
+// memory allocated once per call (gpu/v1/solver.cu:178-298, gpu/v2_twophases/solver.cu:
+// 256-386).  The whole sequence is captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bsj.h"
+#include "bsj_kernels.h"
+
+using namespace bsj;
+
+struct bsj_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sm_count = 0;
+    int max_smem_optin = 0;
+    // grow-only device arena reused by bsj_solve / bsj_solve_batch
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+};
+
+struct bsj_plan {
+    bsj_context* ctx = nullptr;
+    int nseg = 0, ninst = 0, ngroups = 0;
+    int maxN = 0;
+    int total_ranks = 0;
+    int sort_cap = 0, heap_k = 0, heap_chunk = 1, heap_stage = 16;
+    bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
+    int step_grid = 1;
+    std::vector<SegDesc> segs;
+    std::vector<SegState> init;
+    std::vector<int32_t> prefix;
+    std::vector<int32_t> group_init;
+    std::vector<int32_t> seg_group;
+    // device
+    void* mem = nullptr;
+    size_t mem_bytes = 0;
+    bool owns_mem = true;
+    SegDesc* d_segs = nullptr;
+    SegState* d_state = nullptr;
+    SegState* d_state_init = nullptr;
+    int32_t* d_prefix = nullptr;
+    int32_t* d_group = nullptr;
+    int32_t* d_group_init = nullptr;
+    size_t beam_bytes = 0, slot_bytes = 0;
+    StepArgs args{};
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    // timing
+    bool timing = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
+    size_t events_used = 0;
+    int64_t launches = 0;
+    cudaStream_t last_stream = nullptr;
+};
+
+namespace {
+
+constexpr const char* kVersion = "bsj-gb300 0.1.0 (sm_103a)";
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+bsj_status fail(bsj_context* ctx, bsj_status s, const std::string& msg)
+{
+    if (ctx) ctx->err = msg;
+    return s;
+}
+
+bsj_status cuda_fail(bsj_context* ctx, cudaError_t e, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (ctx) ctx->err = m;
+    return (e == cudaErrorMemoryAllocation) ? BSJ_ERR_NOMEM : BSJ_ERR_CUDA;
+}
+
+#define BSJ_CUDA(ctx, call)                                    \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
+    } while (0)
+
+// glibc srand()/rand() state (published algorithm of glibc random_r.c, TYPE_3): r[0] =
+// seed (1 if 0), r[i] = 16807*r[i-1] mod (2^31-1) for i < 31 via Schrage's method,
+// r[i] = r[i-31] for 31..33, r[i] = r[i-31] + r[i-3] afterwards; outputs start at r[344].
+void glibc_rand_state(uint32_t seed, uint32_t ring[34], uint32_t* next_index)
+{
+    std::vector<uint32_t> r(344);
+    int64_t word = (int32_t)(seed == 0 ? 1u : seed);
+    r[0] = (uint32_t)word;
+    for (int k = 1; k < 31; k++) {
+        int64_t hi = word / 127773, lo = word % 127773;
+        word = 16807 * lo - 2836 * hi;
+        if (word < 0) word += 2147483647;
+        r[k] = (uint32_t)word;
+    }
+    for (int k = 31; k < 34; k++) r[k] = r[k - 31];
+    for (int k = 34; k < 344; k++) r[k] = r[k - 31] + r[k - 3];
+    for (int k = 310; k < 344; k++) ring[k % 34] = r[k];
+    *next_index = 344;
+}
+
+bsj_status validate_instance(bsj_context* ctx, const bsj_instance& in)
+{
+    if (in.n < 1 || in.m < 1 || !in.machine || !in.duration)
+        return fail(ctx, BSJ_ERR_INVALID, "instance: n, m must be >= 1 and arrays non-NULL");
+    if (in.n > BSJ_MAX_JOBS || in.m > BSJ_MAX_MACHINES || (int64_t)in.n * in.m > BSJ_MAX_OPS)
+        return fail(ctx, BSJ_ERR_LIMIT, "instance: n <= 128, m <= 64, n*m <= 8192 supported");
+    int64_t total = 0;
+    for (int64_t q = 0; q < (int64_t)in.n * in.m; q++) {
+        if (in.machine[q] < 0 || in.machine[q] >= in.m)
+            return fail(ctx, BSJ_ERR_INVALID, "instance: machine id outside [0, m)");
+        if (in.duration[q] < 0 || in.duration[q] > BSJ_MAX_DURATION)
+            return fail(ctx, BSJ_ERR_LIMIT, "instance: durations must lie in [0, 2^24)");
+        total += in.duration[q];
+    }
+    if (total >= (int64_t)INT32_MAX)
+        return fail(ctx, BSJ_ERR_LIMIT, "instance: total duration must fit int32");
+    return BSJ_OK;
+}
+
+bsj_status ensure_arena(bsj_context* ctx, size_t bytes)
+{
+    if (ctx->arena_bytes >= bytes) return BSJ_OK;
+    if (ctx->arena) cudaFree(ctx->arena);
+    ctx->arena = nullptr;
+    ctx->arena_bytes = 0;
+    size_t want = std::max(bytes, (size_t)1 << 20);
+    cudaError_t e = cudaMalloc(&ctx->arena, want);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(arena)");
+    ctx->arena_bytes = want;
+    return BSJ_OK;
+}
+
+bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, int nbeams,
+                      const bsj_beam* beams, bool use_arena, bsj_plan** out)
+{
+    if (!ctx || !out || ninst < 1 || nbeams < 1 || !insts || !beams)
+        return fail(ctx, BSJ_ERR_INVALID, "plan: null argument or empty batch");
+    for (int i = 0; i < ninst; i++) {
+        bsj_status s = validate_instance(ctx, insts[i]);
+        if (s != BSJ_OK) return s;
+    }
+    bsj_plan* p = new bsj_plan();
+    p->ctx = ctx;
+    p->nseg = nbeams;
+    p->ninst = ninst;
+
+    // op tables: (duration << 8) | machine
+    std::vector<uint32_t> ops;
+    std::vector<int32_t> inst_off(ninst);
+    for (int i = 0; i < ninst; i++) {
+        inst_off[i] = (int32_t)ops.size();
+        for (int64_t q = 0; q < (int64_t)insts[i].n * insts[i].m; q++)
+            ops.push_back(((uint32_t)insts[i].duration[q] << 8) | (uint32_t)insts[i].machine[q]);
+    }
+
+    // bound groups
+    std::vector<int> gid(nbeams);
+    {
+        std::vector<int> user_groups;
+        int next = 0;
+        std::vector<std::pair<int, int>> map;
+        for (int b = 0; b < nbeams; b++) {
+            int g = beams[b].bound_group;
+            if (g < 0) { gid[b] = next++; continue; }
+            auto it = std::find_if(map.begin(), map.end(), [&](const std::pair<int, int>& x) { return x.first == g; });
+            if (it == map.end()) { map.push_back({g, next}); gid[b] = next++; }
+            else gid[b] = it->second;
+        }
+        p->ngroups = next;
+        p->group_init.assign(next, INT32_MAX);
+    }
+
+    // per-beam layout
+    size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0,
+           off_aux = 0, off_seq = 0;
+    int sb_max = 16, aux_max = 16;
+    p->prefix.push_back(0);
+    for (int b = 0; b < nbeams; b++) {
+        const bsj_beam& bm = beams[b];
+        if (bm.instance < 0 || bm.instance >= ninst) { delete p; return fail(ctx, BSJ_ERR_INVALID, "beam: instance index out of range"); }
+        if (bm.mode < BSJ_MODE_V1 || bm.mode > BSJ_MODE_PMS) { delete p; return fail(ctx, BSJ_ERR_INVALID, "beam: unknown mode"); }
+        if (bm.beam_width < 1 || bm.beam_width > BSJ_MAX_BEAM) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "beam: beam_width must lie in [1, 16384]"); }
+        const bsj_instance& in = insts[bm.instance];
+        SegDesc d{};
+        d.n = in.n; d.m = in.m; d.N = in.n * in.m; d.K = bm.beam_width;
+        d.mode = bm.mode; d.seed = bm.seed;
+        d.off_jr = 4 * d.m;
+        d.off_rd = d.off_jr + 4 * d.n;
+        d.off_nx = d.off_rd + d.n;
+        d.off_hdr = (int)align_up((size_t)(d.off_nx + d.n), 4);
+        d.sbytes = (int)align_up((size_t)d.off_hdr + 16, 16);
+        d.words = (d.n + 31) / 32;
+        d.auxbytes = (int)align_up((size_t)(4 + 6 * d.n), 16);
+        d.group = gid[b];
+        d.op_off = inst_off[bm.instance];
+        const size_t K = (size_t)d.K, n = (size_t)d.n, N = (size_t)d.N;
+        const bool gpu = d.mode <= BSJ_MODE_CLEAN;
+        const int nbuf = (d.mode == BSJ_MODE_V1) ? 1 : 2;
+        d.beam_off[0] = (int64_t)off_beam;
+        d.beam_off[1] = (int64_t)(off_beam + (nbuf == 2 ? align_up(K * d.sbytes, 256) : 0));
+        off_beam += nbuf * align_up(K * d.sbytes, 256);
+        d.slot_off = (int64_t)off_slot;
+        if (d.mode == BSJ_MODE_V1) off_slot += align_up(K * n * d.sbytes, 256);
+        d.key_off = (int64_t)off_keys;
+        if (gpu) off_keys += align_up(K * n, 32);
+        d.sel_off = (int64_t)off_sel;
+        off_sel += align_up(K, 64);
+        d.mask_off = (int64_t)off_mask;
+        if (gpu) off_mask += align_up(K * d.words, 64);
+        d.hist_off = (int64_t)off_hist;
+        off_hist += align_up(N * K, 64);
+        d.aux_off = (int64_t)off_aux;
+        if (!gpu) off_aux += align_up(K * d.auxbytes, 256);
+        d.seq_off = (int64_t)off_seq;
+        off_seq += align_up(N, 64);
+        p->segs.push_back(d);
+        p->prefix.push_back(p->prefix.back() + d.K);
+        sb_max = std::max(sb_max, d.sbytes);
+        aux_max = std::max(aux_max, d.auxbytes);
+        p->maxN = std::max(p->maxN, d.N);
+        if (d.mode == BSJ_MODE_V1) p->has_v1 = true;
+        if (d.mode == BSJ_MODE_V1 || d.mode == BSJ_MODE_V2) p->has_zero = true;
+        if (gpu) { p->has_gpu = true; p->sort_cap = std::max(p->sort_cap, d.K); }
+        else { p->has_compat = true; p->heap_k = std::max(p->heap_k, d.K); }
+
+        SegState st{};
+        st.P = 1;
+        st.V = 0;
+        st.bound = bm.best_known;
+        st.best = ~0ull;
+        st.best_cmax = kSentinel;
+        if (!gpu) glibc_rand_state(bm.seed, st.rng, &st.rng_i);
+        p->init.push_back(st);
+        p->group_init[gid[b]] = std::min(p->group_init[gid[b]], bm.best_known);
+        p->seg_group.push_back(gid[b]);
+    }
+    p->total_ranks = p->prefix.back();
+    if (p->has_gpu) {
+        int sc = 1;
+        while (sc < p->sort_cap) sc <<= 1;
+        p->sort_cap = sc;
+    }
+    // ICH/PMS staging: two chunks of parents' child tables next to the heap
+    if (p->has_compat) {
+        size_t budget = (size_t)ctx->max_smem_optin;
+        size_t base = heap_smem_bytes(p->heap_k, 0);
+        if (base + 2 * (size_t)aux_max > budget) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "ICH/PMS beam too wide for shared memory"); }
+        int chunk = (int)std::min<size_t>(32, (budget - base) / (2 * (size_t)aux_max));
+        p->heap_chunk = std::max(1, chunk);
+        p->heap_stage = p->heap_chunk * aux_max;
+    }
+    if (p->has_gpu && select_smem_bytes(p->sort_cap) > (size_t)ctx->max_smem_optin) {
+        delete p;
+        return fail(ctx, BSJ_ERR_LIMIT, "beam too wide for the shared-memory select");
+    }
+
+    // device arena layout
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return at; };
+    const size_t o_segs = take(sizeof(SegDesc) * nbeams);
+    const size_t o_state = take(sizeof(SegState) * nbeams);
+    const size_t o_state_init = take(sizeof(SegState) * nbeams);
+    const size_t o_prefix = take(sizeof(int32_t) * (nbeams + 1));
+    const size_t o_group = take(sizeof(int32_t) * p->ngroups);
+    const size_t o_group_init = take(sizeof(int32_t) * p->ngroups);
+    const size_t o_ops = take(sizeof(uint32_t) * ops.size());
+    const size_t o_beam = take(off_beam);
+    const size_t o_slot = take(off_slot);
+    const size_t o_keys = take(8 * off_keys);
+    const size_t o_sel = take(4 * off_sel);
+    const size_t o_mask = take(4 * off_mask);
+    const size_t o_hist = take(4 * off_hist);
+    const size_t o_aux = take(off_aux);
+    const size_t o_seq = take(4 * off_seq);
+    p->mem_bytes = o;
+    p->beam_bytes = off_beam;
+    p->slot_bytes = off_slot;
+
+    if (use_arena) {
+        bsj_status s = ensure_arena(ctx, o);
+        if (s != BSJ_OK) { delete p; return s; }
+        p->mem = ctx->arena;
+        p->owns_mem = false;
+    } else {
+        cudaError_t e = cudaMalloc(&p->mem, o);
+        if (e != cudaSuccess) { delete p; return cuda_fail(ctx, e, "cudaMalloc(plan)"); }
+        p->owns_mem = true;
+    }
+    uint8_t* base = static_cast<uint8_t*>(p->mem);
+    p->d_segs = reinterpret_cast<SegDesc*>(base + o_segs);
+    p->d_state = reinterpret_cast<SegState*>(base + o_state);
+    p->d_state_init = reinterpret_cast<SegState*>(base + o_state_init);
+    p->d_prefix = reinterpret_cast<int32_t*>(base + o_prefix);
+    p->d_group = reinterpret_cast<int32_t*>(base + o_group);
+    p->d_group_init = reinterpret_cast<int32_t*>(base + o_group_init);
+
+    StepArgs& a = p->args;
+    a.segs = p->d_segs;
+    a.st = p->d_state;
+    a.rank_prefix = p->d_prefix;
+    a.nseg = nbeams;
+    a.total_ranks = p->total_ranks;
+    a.sb_max = sb_max;
+    a.beam_pool = base + o_beam;
+    a.slot_pool = base + o_slot;
+    a.keys = reinterpret_cast<unsigned long long*>(base + o_keys);
+    a.sel = reinterpret_cast<uint32_t*>(base + o_sel);
+    a.masks = reinterpret_cast<uint32_t*>(base + o_mask);
+    a.hist = reinterpret_cast<uint32_t*>(base + o_hist);
+    a.aux_pool = base + o_aux;
+    a.ops = reinterpret_cast<const uint32_t*>(base + o_ops);
+    a.group_best = p->d_group;
+    a.seq_pool = reinterpret_cast<int32_t*>(base + o_seq);
+
+    // uploads (synchronous: the host vectors are pageable)
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_segs, p->segs.data(), sizeof(SegDesc) * nbeams, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * nbeams, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_prefix, p->prefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_ops, ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        if (p->owns_mem) cudaFree(p->mem);
+        delete p;
+        return cuda_fail(ctx, e, "plan upload");
+    }
+
+    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16), sb_max);
+    if (e != cudaSuccess) {
+        if (p->owns_mem) cudaFree(p->mem);
+        delete p;
+        return cuda_fail(ctx, e, "configure kernels");
+    }
+    // warps of k_step: one per rank, 8 per CTA, up to 8 CTAs per SM resident
+    int want = (p->total_ranks + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
+    p->step_grid = std::max(1, std::min(want, ctx->sm_count * 8));
+    *out = p;
+    return BSJ_OK;
+}
+
+cudaEvent_t* next_events(bsj_plan* p, int cls)
+{
+    if (p->events_used == p->events.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        p->events.push_back({cls, {a, b}});
+    }
+    auto& ev = p->events[p->events_used++];
+    ev.first = cls;
+    return &ev.second.first;
+}
+
+// Enqueue one run of the plan on `s`.
+cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s)
+{
+    const StepArgs& a = p->args;
+    cudaError_t e;
+    p->launches = 0;
+    p->events_used = 0;
+    auto timed = [&](int cls, auto&& fn) -> cudaError_t {
+        if (!p->timing) { p->launches++; return fn(); }
+        cudaEvent_t* ev = next_events(p, cls);
+        cudaEventRecord(ev[0], s);
+        cudaError_t r = fn();
+        cudaEventRecord(ev[1], s);
+        p->launches++;
+        return r;
+    };
+    e = cudaMemcpyAsync(p->d_state, p->d_state_init, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(p->d_group, p->d_group_init, sizeof(int32_t) * p->ngroups, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (p->has_zero) {
+        // v1 / v2 read never-written slots; the reference sees a fresh allocation (zeros)
+        e = cudaMemsetAsync(a.beam_pool, 0, p->beam_bytes, s);
+        if (e != cudaSuccess) return e;
+        if (p->slot_bytes) e = cudaMemsetAsync(a.slot_pool, 0, p->slot_bytes, s);
+        if (e != cudaSuccess) return e;
+    }
+    e = timed(0, [&] { return launch_step(a, -1, p->step_grid, s); });
+    if (e != cudaSuccess) return e;
+    for (int lv = 0; lv < p->maxN; lv++) {
+        if (p->has_gpu) {
+            e = timed(1, [&] { return launch_select(a, lv, p->sort_cap, s); });
+            if (e != cudaSuccess) return e;
+        }
+        if (p->has_compat) {
+            e = timed(2, [&] { return launch_heap(a, lv, p->heap_k, p->heap_chunk, p->heap_stage, s); });
+            if (e != cudaSuccess) return e;
+        }
+        if (lv < p->maxN - 1) {
+            if (p->has_v1) {
+                e = timed(3, [&] { return launch_gather_v1(a, lv, p->step_grid, s); });
+                if (e != cudaSuccess) return e;
+            }
+            e = timed(0, [&] { return launch_step(a, lv, p->step_grid, s); });
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return timed(4, [&] { return launch_finalize(a, s); });
+}
+
+}  // namespace
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+extern "C" {
+
+const char* bsj_version(void) { return kVersion; }
+
+const char* bsj_status_string(bsj_status s)
+{
+    switch (s) {
+    case BSJ_OK: return "ok";
+    case BSJ_ERR_INVALID: return "invalid argument";
+    case BSJ_ERR_LIMIT: return "size outside the supported limits";
+    case BSJ_ERR_CUDA: return "CUDA error";
+    case BSJ_ERR_NOMEM: return "out of memory";
+    case BSJ_ERR_DEVICE: return "device-side consistency check failed";
+    }
+    return "unknown status";
+}
+
+bsj_status bsj_create(bsj_context** out, int device)
+{
+    if (!out) return BSJ_ERR_INVALID;
+    *out = nullptr;
+    bsj_context* ctx = new bsj_context();
+    cudaError_t e;
+    if (device < 0) {
+        e = cudaGetDevice(&device);
+        if (e != cudaSuccess) { bsj_status s = cuda_fail(ctx, e, "cudaGetDevice"); delete ctx; return s; }
+    }
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete ctx; return BSJ_ERR_CUDA; }
+    ctx->device = device;
+    *out = ctx;
+    return BSJ_OK;
+}
+
+void bsj_destroy(bsj_context* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* bsj_last_error(const bsj_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+bsj_status bsj_plan_create(bsj_context* ctx, int num_instances, const bsj_instance* instances,
+                           int num_beams, const bsj_beam* beams, bsj_plan** out)
+{
+    if (!ctx) return BSJ_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    return plan_build(ctx, num_instances, instances, num_beams, beams, false, out);
+}
+
+bsj_status bsj_plan_run(bsj_plan* p, void* stream)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    bsj_context* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    p->last_stream = s;
+    if (p->timing) {
+        cudaError_t e = enqueue_run(p, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "plan run");
+        return BSJ_OK;
+    }
+    if (!p->graph) {
+        // capture once on the context's stream, replay on any stream
+        cudaStream_t cap = ctx->stream;
+        cudaGraph_t g = nullptr;
+        BSJ_CUDA(ctx, cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_run(p, cap);
+        cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ctx, e, "plan capture"); }
+        if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&p->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { p->graph = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+    }
+    BSJ_CUDA(ctx, cudaGraphLaunch(p->graph, s));
+    return BSJ_OK;
+}
+
+bsj_status bsj_plan_results(bsj_plan* p, bsj_result* results)
+{
+    if (!p || !results) return BSJ_ERR_INVALID;
+    bsj_context* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = p->last_stream ? p->last_stream : ctx->stream;
+    BSJ_CUDA(ctx, cudaStreamSynchronize(s));
+    std::vector<SegState> st(p->nseg);
+    std::vector<int32_t> grp(p->ngroups);
+    BSJ_CUDA(ctx, cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost));
+    BSJ_CUDA(ctx, cudaMemcpy(grp.data(), p->d_group, sizeof(int32_t) * p->ngroups, cudaMemcpyDeviceToHost));
+    bsj_status status = BSJ_OK;
+    for (int b = 0; b < p->nseg; b++) {
+        const SegDesc& d = p->segs[b];
+        bsj_result& r = results[b];
+        r.makespan = st[b].makespan;
+        r.found = st[b].found;
+        r.expanded = st[b].expanded;
+        r.slots = st[b].slots;
+        r.levels = st[b].levels;
+        r.group_best = grp[p->seg_group[b]];
+        if (r.sequence) {
+            BSJ_CUDA(ctx, cudaMemcpy(r.sequence, p->args.seq_pool + d.seq_off, sizeof(int32_t) * d.N, cudaMemcpyDeviceToHost));
+        }
+        if (st[b].status != 0) {
+            status = BSJ_ERR_DEVICE;
+            ctx->err = "beam " + std::to_string(b) + ": device status " + std::to_string(st[b].status);
+        }
+    }
+    return status;
+}
+
+void bsj_plan_destroy(bsj_plan* p)
+{
+    if (!p) return;
+    cudaSetDevice(p->ctx->device);
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (auto& ev : p->events) {
+        cudaEventDestroy(ev.second.first);
+        cudaEventDestroy(ev.second.second);
+    }
+    if (p->owns_mem && p->mem) cudaFree(p->mem);
+    delete p;
+}
+
+int64_t bsj_plan_launches(const bsj_plan* p)
+{
+    if (!p) return 0;
+    // fixed by the plan shape: 1 + maxN*(select? + heap?) + (maxN-1)*(gather_v1? + step) + 1
+    int64_t per = (p->has_gpu ? 1 : 0) + (p->has_compat ? 1 : 0);
+    int64_t n = 2 + (int64_t)p->maxN * per + (int64_t)(p->maxN - 1) * (1 + (p->has_v1 ? 1 : 0));
+    return n;
+}
+
+bsj_status bsj_plan_stats(const bsj_plan* p, double* step_bytes, int64_t* expanded, int64_t* step_launches)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    std::vector<SegState> st(p->nseg);
+    cudaSetDevice(p->ctx->device);
+    cudaError_t e = cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return BSJ_ERR_CUDA;
+    double bytes = 0.0;
+    int64_t ex = 0;
+    for (int b = 0; b < p->nseg; b++) {
+        const SegDesc& d = p->segs[b];
+        bytes += (double)st[b].materialized * (2.0 * d.sbytes + 8.0) + 8.0 * (double)st[b].expanded;
+        ex += st[b].expanded;
+    }
+    if (step_bytes) *step_bytes = bytes;
+    if (expanded) *expanded = ex;
+    if (step_launches) *step_launches = p->maxN;  // k_step(-1) .. k_step(maxN-2)
+    return BSJ_OK;
+}
+
+bsj_status bsj_plan_set_timing(bsj_plan* p, int enable)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    p->timing = enable != 0;
+    return BSJ_OK;
+}
+
+bsj_status bsj_plan_kernel_ms(const bsj_plan* p, float* ms, int64_t* launches, int count)
+{
+    if (!p || !ms) return BSJ_ERR_INVALID;
+    for (int i = 0; i < count; i++) { ms[i] = 0.f; if (launches) launches[i] = 0; }
+    cudaSetDevice(p->ctx->device);
+    for (size_t k = 0; k < p->events_used; k++) {
+        const auto& ev = p->events[k];
+        float t = 0.f;
+        cudaError_t e = cudaEventSynchronize(ev.second.second);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev.second.first, ev.second.second);
+        if (e != cudaSuccess) return BSJ_ERR_CUDA;
+        if (ev.first < count) {
+            ms[ev.first] += t;
+            if (launches) launches[ev.first]++;
+        }
+    }
+    return BSJ_OK;
+}
+
+bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instance* instances,
+                           int num_beams, const bsj_beam* beams, bsj_result* results, void* stream)
+{
+    if (!ctx || !results) return BSJ_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    bsj_plan* p = nullptr;
+    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, true, &p);
+    if (s != BSJ_OK) return s;
+    // eager launches: a one-shot plan gains nothing from graph capture
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    p->last_stream = st;
+    cudaError_t e = enqueue_run(p, st);
+    if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
+    s = bsj_plan_results(p, results);
+    bsj_plan_destroy(p);
+    return s;
+}
+
+bsj_status bsj_solve(bsj_context* ctx, const bsj_instance* inst, const bsj_beam* beam,
+                     bsj_result* result, void* stream)
+{
+    if (!ctx || !inst || !beam || !result) return BSJ_ERR_INVALID;
+    bsj_beam b = *beam;
+    b.instance = 0;
+    return bsj_solve_batch(ctx, 1, inst, 1, &b, result, stream);
+}
+
+bsj_status bsj_solve_iterations(bsj_context* ctx, const bsj_instance* inst, int mode, int beam_width,
+                                int num_beams, int iterations, const uint32_t* seeds,
+                                int32_t initial_bound, int32_t* best, int32_t* best_sequence, void* stream)
+{
+    if (!ctx || !inst || !seeds || num_beams < 1 || iterations < 1) return BSJ_ERR_INVALID;
+    int32_t bound = initial_bound;
+    int32_t overall = initial_bound;
+    std::vector<int32_t> seq((size_t)inst->n * inst->m);
+    bool have_seq = false;
+    std::vector<bsj_beam> beams(num_beams);
+    std::vector<bsj_result> res(num_beams);
+    std::vector<std::vector<int32_t>> seqs(num_beams, std::vector<int32_t>(seq.size()));
+    for (int it = 0; it < iterations; it++) {
+        for (int b = 0; b < num_beams; b++) {
+            beams[b] = bsj_beam{mode, beam_width, bound, seeds[(size_t)it * num_beams + b], 0, 0};
+            res[b] = bsj_result{};
+            res[b].sequence = seqs[b].data();
+        }
+        bsj_status s = bsj_solve_batch(ctx, 1, inst, num_beams, beams.data(), res.data(), stream);
+        if (s != BSJ_OK) return s;
+        // MPI_Allreduce(MIN) of the ranks' bests (gpu/v1/main.cu:66-70)
+        for (int b = 0; b < num_beams; b++) {
+            if (res[b].makespan < overall) {
+                overall = res[b].makespan;
+                if (res[b].found) { seq = seqs[b]; have_seq = true; }
+            }
+        }
+        bound = overall;
+    }
+    if (best) *best = overall;
+    if (best_sequence) {
+        if (have_seq) std::memcpy(best_sequence, seq.data(), seq.size() * sizeof(int32_t));
+        else std::memset(best_sequence, 0, seq.size() * sizeof(int32_t));
+    }
+    return BSJ_OK;
+}
+
+}  // extern "C"

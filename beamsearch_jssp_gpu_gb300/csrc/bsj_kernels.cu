@@ -1,0 +1,1032 @@
+// bsj_kernels.cu -- the level kernels of the beam search, sm_103a.
+//
+// One search level (reference: the body of the level loop, gpu/v1/solver.cu:234-275 and
+// gpu/v2_twophases/solver.cu:315-363) runs as
+//
+//   k_select(s)      per beam: exact top-K of the level's candidate keys + stable order
+//                    (replaces cub::DeviceRadixSort::SortPairs over all P*n slots)
+//   k_heap(s)        per beam, ICH/PMS modes: the CPU solvers' bounded heap, in order
+//   k_gather_v1(s)   v1 mode only: copy the selected child slots into the beam
+//   k_step(s)        warp per survivor: materialise the survivor from its parent (fused
+//                    gather), then expand it for level s+1: pivot machine by ballot,
+//                    child makespan, fp32 score, key emission
+//
+// Integer work only, apart from the fp32 (gpu modes) / fp64 (PMS) score, computed with
+// the reference's operations in its order.
+#include "bsj_kernels.h"
+
+namespace bsj {
+
+#define FULL_MASK 0xFFFFFFFFu
+
+// ------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ int find_seg(const int32_t* prefix, int nseg, int flat)
+{
+    int lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(prefix + mid) <= flat) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t op_info(const uint32_t* ops, int op_off, int j, int m, int k)
+{
+    return __ldg(ops + op_off + j * m + k);
+}
+
+// Root state: first op of every job ready in job order (gpu_snapshot.cuh:34-44,
+// jssp_types.h:61-72).
+__device__ void build_root(uint8_t* sb, const Lay& L, int lane)
+{
+    uint4 z = make_uint4(0, 0, 0, 0);
+    for (int q = lane; q < (L.sbytes >> 4); q += 32) reinterpret_cast<uint4*>(sb)[q] = z;
+    __syncwarp();
+    for (int j = lane; j < L.n; j += 32) RD(sb, L)[j] = (uint8_t)j;
+    if (lane == 0) {
+        *H_R(sb, L) = (uint16_t)L.n;
+        *H_NS(sb, L) = 0;
+        *H_CMAX(sb, L) = 0;
+        *H_LIN(sb, L) = kMark;
+        *H_STAMP(sb, L) = 0;
+    }
+    __syncwarp();
+}
+
+// Ready ops of the state in `sb`, lane-major: position i = lane + 32*q.
+struct ReadyOps {
+    int r;
+    int job[4], k[4], mc[4], du[4];
+};
+
+__device__ __forceinline__ void load_ready(uint8_t* sb, const Lay& L, const uint32_t* ops,
+                                           int op_off, int lane, ReadyOps& R)
+{
+    R.r = *H_R(sb, L);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        int i = lane + 32 * q;
+        R.mc[q] = -1;
+        R.job[q] = 0;
+        R.k[q] = 0;
+        R.du[q] = 0;
+        if (i < R.r) {
+            int j = RD(sb, L)[i];
+            int k = NX(sb, L)[j];
+            uint32_t o = op_info(ops, op_off, j, L.m, k);
+            R.job[q] = j;
+            R.k[q] = k;
+            R.mc[q] = (int)(o & 0xFFu);
+            R.du[q] = (int)(o >> 8);
+        }
+    }
+}
+
+// Pivot machine and candidate ballot (gpu/v1/solver.cu:47-69): thread 0 of the reference
+// hashes (seed + rank), takes that ready op's machine, and lists the ready ops on that
+// machine in ready-list order; here every lane tests its ops and a ballot gives each
+// candidate its branch index b.
+struct Cands {
+    unsigned bal[4];
+    int bidx[4];
+    int cnt;
+    int pm;
+};
+
+__device__ __forceinline__ void pivot_candidates(const ReadyOps& R, uint32_t seed_t, uint32_t c,
+                                                 int lane, Cands& C)
+{
+    C.cnt = 0;
+    C.pm = -1;
+#pragma unroll
+    for (int q = 0; q < 4; q++) { C.bal[q] = 0; C.bidx[q] = 0; }
+    if (R.r <= 0) return;
+    uint32_t h = pivot_hash(seed_t + c);
+    int pp = (int)(h % (uint32_t)R.r);
+    int qp = pp >> 5;
+    int mine = (qp == 0) ? R.mc[0] : (qp == 1) ? R.mc[1] : (qp == 2) ? R.mc[2] : R.mc[3];
+    int pm = __shfl_sync(FULL_MASK, mine, pp & 31);
+    unsigned lt = (1u << lane) - 1u;
+    int acc = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        C.bal[q] = __ballot_sync(FULL_MASK, (lane + 32 * q < R.r) && R.mc[q] == pm);
+        C.bidx[q] = acc + __popc(C.bal[q] & lt);
+        acc += __popc(C.bal[q]);
+    }
+    C.cnt = acc;
+    C.pm = pm;
+}
+
+// Job-predecessor finish of op (job j, step k): jssp_types.h:82 / gpu_snapshot.cuh:58
+// read op_finish[op-1] unless op % m == 1.  For m >= 2 that is "job j's previous op, or 0
+// for its first op"; for m == 1 the test never holds and op-1 is job j-1's op.
+__device__ __forceinline__ int pred_finish(uint8_t* sb, const Lay& L, int j, int k)
+{
+    if (L.m == 1) return j > 0 ? JR(sb, L)[j - 1] : 0;
+    return k == 0 ? 0 : JR(sb, L)[j];
+}
+
+// Apply "schedule the ready op at position i" to the state in `b` (warp-collective):
+// removal from the ready list (swap-with-last for the gpu modes, gpu/v1/solver.cu:100-106;
+// order-preserving erase for ICH/PMS, cpu/v0_ich/solver.cpp:29, cpu/v1_pms/solver.cpp:44-46),
+// then dev_schedule_operation (gpu_snapshot.cuh:47-70) and the makespan.
+__device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int op_off, int i,
+                            bool erase, uint32_t lineage, uint32_t stamp, int lane)
+{
+    const int r = *H_R(b, L);
+    const int j = RD(b, L)[i];
+    const int k = NX(b, L)[j];
+    const uint32_t o = op_info(ops, op_off, j, L.m, k);
+    const int mc = (int)(o & 0xFFu);
+    const int pred = pred_finish(b, L, j, k);
+    const int tr = TR(b)[mc];
+    const int fin = (tr > pred ? tr : pred) + (int)(o >> 8);
+    __syncwarp();
+    if (erase) {
+        uint8_t v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int t = lane + 32 * q;
+            v[q] = (t >= i && t < r - 1) ? RD(b, L)[t + 1] : 0;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int t = lane + 32 * q;
+            if (t >= i && t < r - 1) RD(b, L)[t] = v[q];
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        TR(b)[mc] = fin;
+        JR(b, L)[j] = fin;
+        if (!erase) RD(b, L)[i] = RD(b, L)[r - 1];
+        int rr = r - 1;
+        if (k + 1 < L.m) RD(b, L)[rr++] = (uint8_t)j;
+        NX(b, L)[j] = (uint8_t)(k + 1);
+        *H_R(b, L) = (uint16_t)rr;
+        *H_NS(b, L) = (uint16_t)(*H_NS(b, L) + 1);
+        int cm = *H_CMAX(b, L);
+        *H_CMAX(b, L) = cm > fin ? cm : fin;
+        *H_LIN(b, L) = lineage;
+        *H_STAMP(b, L) = stamp;
+    }
+    __syncwarp();
+}
+
+// ------------------------------------------------------------------------------------
+// Expansion of one state for level t (gpu modes): kernel_expand_beam_layer /
+// kernel_score_candidates (gpu/v1/solver.cu:72-127, v2 :68-123) without the per-thread
+// snapshot copy -- a child's makespan needs only tr[pivot machine], the job's
+// predecessor finish and the parent makespan.
+// ------------------------------------------------------------------------------------
+__device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc& d,
+                           SegState& st, const StepArgs& a, int c, int t, int lane)
+{
+    ReadyOps R;
+    load_ready(sb, L, a.ops, d.op_off, lane, R);
+    const uint32_t seed_t = d.seed + (uint32_t)t;
+    Cands C;
+    pivot_candidates(R, seed_t, (uint32_t)c, lane, C);
+    const int ns1 = *H_NS(sb, L) + 1;
+    const int pcmax = *H_CMAX(sb, L);
+    const int bound = st.bound;
+    const int trp = (C.pm >= 0) ? TR(sb)[C.pm] : 0;
+    const bool last = (t == d.N - 1);
+
+    unsigned long long key[4];
+    unsigned vb[4];
+    uint32_t wacc[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        bool valid = false;
+        key[q] = 0ull;
+        if ((C.bal[q] >> lane) & 1u) {
+            const int pred = pred_finish(sb, L, R.job[q], R.k[q]);
+            const int fin = (trp > pred ? trp : pred) + R.du[q];
+            const int cm = pcmax > fin ? pcmax : fin;
+            valid = cm < bound;   // gpu/v1/solver.cu:120
+            if (valid) {
+                const int b = C.bidx[q];
+                const float sc = gpu_score(cm, ns1, seed_t, (uint32_t)c, (uint32_t)b);
+                const uint32_t slot = (uint32_t)(c * L.n + b);
+                key[q] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
+                wacc[b >> 5] |= 1u << (b & 31);
+                if (last && ns1 == d.N) {
+                    atomicMin(&st.best, ((unsigned long long)(uint32_t)cm << 32) |
+                                            ((unsigned long long)slot << 8) | (uint32_t)R.job[q]);
+                    atomicMin(a.group_best + d.group, cm);
+                }
+            }
+        }
+        vb[q] = __ballot_sync(FULL_MASK, valid);
+    }
+    int nv = __popc(vb[0]) + __popc(vb[1]) + __popc(vb[2]) + __popc(vb[3]);
+    int base = 0;
+    if (lane == 0 && nv > 0) base = atomicAdd(&st.V, nv);
+    base = __shfl_sync(FULL_MASK, base, 0);
+    const unsigned lt = (1u << lane) - 1u;
+    int acc = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if ((vb[q] >> lane) & 1u) a.keys[d.key_off + base + acc + __popc(vb[q] & lt)] = key[q];
+        acc += __popc(vb[q]);
+    }
+    for (int w = 0; w < d.words; w++) {
+        uint32_t word = __reduce_or_sync(FULL_MASK, wacc[w & 3]);
+        if (lane == 0) a.masks[d.mask_off + (int64_t)c * d.words + w] = word;
+    }
+
+    if (d.mode == MODE_V1 && nv > 0) {
+        // kernel_expand_beam_layer also writes every scored child's snapshot into its
+        // slot c*n+b (gpu/v1/solver.cu:129-145); slots it skips keep older content.
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            unsigned bits = vb[q];
+            while (bits) {
+                const int l = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const int i = 32 * q + l;
+                const int b = __shfl_sync(FULL_MASK, C.bidx[q], l);
+                const int j = __shfl_sync(FULL_MASK, R.job[q], l);
+                warp_copy_smem(cb, sb, L.sbytes, lane);
+                __syncwarp();
+                apply_child(cb, L, a.ops, d.op_off, i, false, ((uint32_t)c << 8) | (uint32_t)j,
+                            (uint32_t)(t + 1), lane);
+                warp_store(a.slot_pool + d.slot_off + (int64_t)(c * L.n + b) * L.sbytes, cb, L.sbytes, lane);
+                __syncwarp();
+            }
+        }
+    }
+}
+
+// ICH / PMS: per ready position, the child's makespan, machine and job; the ordered
+// serial part (rand() draws, heap) runs in k_heap (cpu/v0_ich/solver.cpp:22-39,
+// cpu/v1_pms/solver.cpp:26-62).
+__device__ void expand_compat(uint8_t* sb, const Lay& L, const SegDesc& d, const StepArgs& a,
+                              int c, int lane)
+{
+    ReadyOps R;
+    load_ready(sb, L, a.ops, d.op_off, lane, R);
+    const int pcmax = *H_CMAX(sb, L);
+    uint8_t* base = a.aux_pool + d.aux_off + (int64_t)c * d.auxbytes;
+    int32_t* cc = reinterpret_cast<int32_t*>(base + 4);
+    uint8_t* cmv = base + 4 + 4 * L.n;
+    uint8_t* jb = base + 4 + 5 * L.n;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        int i = lane + 32 * q;
+        if (i < R.r) {
+            const int pred = pred_finish(sb, L, R.job[q], R.k[q]);
+            const int tr = TR(sb)[R.mc[q]];
+            const int fin = (tr > pred ? tr : pred) + R.du[q];
+            cc[i] = pcmax > fin ? pcmax : fin;
+            cmv[i] = (uint8_t)R.mc[q];
+            jb[i] = (uint8_t)R.job[q];
+        }
+    }
+    if (lane == 0) *reinterpret_cast<uint32_t*>(base) = (uint32_t)R.r;
+}
+
+// ------------------------------------------------------------------------------------
+// k_step: materialise level s+1 (warp per survivor) and expand it.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int s)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint8_t* sb = smem + (size_t)warp * 2 * a.sb_max;
+    uint8_t* cb = sb + a.sb_max;
+    const int nw = gridDim.x * kWarpsPerStepCta;
+    for (int flat = blockIdx.x * kWarpsPerStepCta + warp; flat < a.total_ranks; flat += nw) {
+        const int seg = find_seg(a.rank_prefix, a.nseg, flat);
+        const SegDesc& d = a.segs[seg];
+        if (s >= d.N - 1) continue;
+        SegState& st = a.st[seg];
+        const int r = flat - __ldg(a.rank_prefix + seg);
+        const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
+        if (r >= P) continue;
+        const Lay L(d);
+        const int mode = d.mode;
+        if (mode == MODE_V1) {
+            uint8_t* beam = a.beam_pool + d.beam_off[0];
+            if (s < 0) {
+                build_root(sb, L, lane);
+                warp_store(beam, sb, L.sbytes, lane);
+            } else {
+                warp_load(sb, beam + (int64_t)r * L.sbytes, L.sbytes, lane);
+            }
+            __syncwarp();
+            expand_gpu(sb, cb, L, d, st, a, r, s + 1, lane);
+            continue;
+        }
+        uint8_t* child = a.beam_pool + d.beam_off[(s + 1) & 1];
+        if (s < 0) {
+            build_root(sb, L, lane);
+            warp_store(child, sb, L.sbytes, lane);
+        } else {
+            const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
+            const uint32_t e = __ldg(a.sel + d.sel_off + r);
+            uint32_t* hrow = a.hist + d.hist_off + (int64_t)s * d.K;
+            if (mode == MODE_ICH || mode == MODE_PMS) {
+                const int c = (int)(e >> 8), i = (int)(e & 0xFFu);
+                warp_load(sb, parent + (int64_t)c * L.sbytes, L.sbytes, lane);
+                __syncwarp();
+                const int j = RD(sb, L)[i];
+                apply_child(sb, L, a.ops, d.op_off, i, true, ((uint32_t)c << 8) | (uint32_t)j,
+                            (uint32_t)(s + 1), lane);
+                warp_store(child + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
+                if (lane == 0) hrow[r] = ((uint32_t)c << 8) | (uint32_t)j;
+            } else {
+                const uint32_t slot = e & ~kFillerFlag;
+                const int c = (int)(slot / (uint32_t)L.n), b = (int)(slot % (uint32_t)L.n);
+                warp_load(sb, parent + (int64_t)c * L.sbytes, L.sbytes, lane);
+                __syncwarp();
+                ReadyOps R;
+                load_ready(sb, L, a.ops, d.op_off, lane, R);
+                Cands C;
+                pivot_candidates(R, d.seed + (uint32_t)s, (uint32_t)c, lane, C);
+                if (b < C.cnt) {
+                    // kernel_materialize_topk (gpu/v2_twophases/solver.cu:193-252)
+                    int i = -1, j = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        unsigned hit = __ballot_sync(FULL_MASK, ((C.bal[q] >> lane) & 1u) && C.bidx[q] == b);
+                        if (hit) {
+                            const int l = __ffs(hit) - 1;
+                            i = 32 * q + l;
+                            j = __shfl_sync(FULL_MASK, R.job[q], l);
+                        }
+                    }
+                    apply_child(sb, L, a.ops, d.op_off, i, false, ((uint32_t)c << 8) | (uint32_t)j,
+                                (uint32_t)(s + 1), lane);
+                    warp_store(child + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
+                    if (lane == 0) hrow[r] = ((uint32_t)c << 8) | (uint32_t)j;
+                } else {
+                    // filler rank: v2 leaves the ping-pong slot as it was (:191)
+                    if (mode == MODE_CLEAN && lane == 0) atomicOr(&st.status, kStatusBadSelect);
+                    __syncwarp();
+                    warp_load(sb, child + (int64_t)r * L.sbytes, L.sbytes, lane);
+                    if (lane == 0) hrow[r] = kMark;
+                }
+            }
+        }
+        __syncwarp();
+        if (mode == MODE_ICH || mode == MODE_PMS) expand_compat(sb, L, d, a, r, lane);
+        else expand_gpu(sb, cb, L, d, st, a, r, s + 1, lane);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// k_gather_v1: kernel_gather_topk (gpu/v1/solver.cu:160-176), warp per survivor, 16-byte
+// vector copies.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a, int s)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = gridDim.x * kWarpsPerStepCta;
+    for (int flat = blockIdx.x * kWarpsPerStepCta + warp; flat < a.total_ranks; flat += nw) {
+        const int seg = find_seg(a.rank_prefix, a.nseg, flat);
+        const SegDesc& d = a.segs[seg];
+        if (d.mode != MODE_V1 || s >= d.N - 1) continue;
+        const int r = flat - __ldg(a.rank_prefix + seg);
+        if (r >= a.st[seg].P) continue;
+        const uint32_t slot = __ldg(a.sel + d.sel_off + r) & ~kFillerFlag;
+        const uint8_t* src = a.slot_pool + d.slot_off + (int64_t)slot * d.sbytes;
+        uint8_t* dst = a.beam_pool + d.beam_off[0] + (int64_t)r * d.sbytes;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (int q = lane; q < (d.sbytes >> 4); q += 32) d4[q] = s4[q];
+        if (lane == 0) {
+            const uint32_t lin = *reinterpret_cast<const uint32_t*>(src + d.off_hdr + 8);
+            const uint32_t stamp = *reinterpret_cast<const uint32_t*>(src + d.off_hdr + 12);
+            a.hist[d.hist_off + (int64_t)s * d.K + r] = (stamp == (uint32_t)(s + 1)) ? lin : kMark;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// k_select: exact top-K + stable order per beam (gpu modes).
+//
+// The reference sorts all P*n (score, slot) pairs with a stable radix sort and keeps the
+// first min(P*n, K) (gpu/v1/solver.cu:255-274).  Scores of skipped slots are 1e9f, above
+// every real score, so the kept list is: the real candidates in ascending
+// (score bits, slot) order, then -- only when fewer than min(P*n,K) are real -- the
+// lowest-numbered skipped slots ("fillers").  Keys are unique 64-bit
+// (score bits << 32 | slot), so the top-K set is exact: an MSD radix select finds the
+// K-th key, survivors are compacted and bitonic-sorted in shared memory.
+// ------------------------------------------------------------------------------------
+struct SelSmem {
+    uint32_t* hist;           // [32][256]
+    uint32_t* tot;            // [256]
+    unsigned long long* red;  // [64]
+    int* misc;                // [64]
+    unsigned long long* sortbuf;
+};
+
+__device__ __forceinline__ SelSmem sel_smem(uint8_t* base)
+{
+    SelSmem s;
+    s.hist = reinterpret_cast<uint32_t*>(base);
+    s.tot = s.hist + 32 * 256;
+    s.red = reinterpret_cast<unsigned long long*>(s.tot + 256);
+    s.misc = reinterpret_cast<int*>(s.red + 64);
+    s.sortbuf = reinterpret_cast<unsigned long long*>(s.misc + 64);
+    return s;
+}
+
+size_t select_smem_bytes(int sort_cap)
+{
+    return (size_t)(32 * 256 + 256) * 4 + 64 * 8 + 64 * 4 + (size_t)sort_cap * 8;
+}
+
+// Block-wide exclusive scan of one int per thread; returns the prefix, *total the sum.
+__device__ int block_exclusive_scan(int v, int* total, int* warp_sums)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nwarps ? warp_sums[lane] : 0;
+        int ws = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(FULL_MASK, ws, o);
+            if (lane >= o) ws += y;
+        }
+        warp_sums[32 + lane] = ws - w;
+        if (lane == 31) warp_sums[64] = ws;
+    }
+    __syncthreads();
+    int res = warp_sums[32 + warp] + x - v;
+    *total = warp_sums[64];
+    __syncthreads();
+    return res;
+}
+
+template <bool REG>
+__device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int s, uint8_t* smem)
+{
+    constexpr int KPT = 16;
+    SelSmem S = sel_smem(smem);
+    int* wsum = reinterpret_cast<int*>(S.hist);  // scan scratch (hist is free outside passes)
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int P = st.P, V = st.V, n = d.n, K = d.K;
+    const int total = P * n;
+    int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
+    const int R = V < keff ? V : keff;
+    const unsigned long long* keys = a.keys + d.key_off;
+
+    unsigned long long kr[REG ? KPT : 1];
+    if (REG) {
+#pragma unroll
+        for (int q = 0; q < (REG ? KPT : 1); q++) {
+            int idx = tid + q * nthr;
+            kr[q] = idx < V ? keys[idx] : ~0ull;
+        }
+    }
+
+    unsigned long long pmask = 0ull, prefix = 0ull;
+    if (V > R && R > 0) {
+        // --- min / max -> highest differing bit ---
+        unsigned long long mn = ~0ull, mx = 0ull;
+        if (REG) {
+#pragma unroll
+            for (int q = 0; q < (REG ? KPT : 1); q++)
+                if (tid + q * nthr < V) { mn = min(mn, kr[q]); mx = max(mx, kr[q]); }
+        } else {
+            for (int idx = tid; idx < V; idx += nthr) { unsigned long long k = keys[idx]; mn = min(mn, k); mx = max(mx, k); }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+            mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+        }
+        if (lane == 0) { S.red[warp] = mn; S.red[32 + warp] = mx; }
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long a0 = ~0ull, a1 = 0ull;
+            for (int w = 0; w < (nthr >> 5); w++) { a0 = min(a0, S.red[w]); a1 = max(a1, S.red[32 + w]); }
+            S.red[0] = a0;
+            S.red[32] = a1;
+        }
+        __syncthreads();
+        mn = S.red[0];
+        mx = S.red[32];
+        __syncthreads();
+        const int hb = 63 - __clzll((long long)(mn ^ mx));
+        pmask = (hb >= 63) ? 0ull : ~((2ull << hb) - 1ull);
+        prefix = mn & pmask;
+        int shift = hb + 1;
+        int rem = R;
+        while (shift > 0) {
+            const int db = shift < 8 ? shift : 8;
+            shift -= db;
+            const unsigned dm = (1u << db) - 1u;
+            for (int t = tid; t < 32 * 256; t += nthr) S.hist[t] = 0;
+            __syncthreads();
+            uint32_t* hw = S.hist + warp * 256;
+            if (REG) {
+#pragma unroll
+                for (int q = 0; q < (REG ? KPT : 1); q++) {
+                    unsigned long long k = kr[q];
+                    if (tid + q * nthr < V && (k & pmask) == prefix) atomicAdd(hw + ((unsigned)(k >> shift) & dm), 1u);
+                }
+            } else {
+                for (int idx = tid; idx < V; idx += nthr) {
+                    unsigned long long k = keys[idx];
+                    if ((k & pmask) == prefix) atomicAdd(hw + ((unsigned)(k >> shift) & dm), 1u);
+                }
+            }
+            __syncthreads();
+            for (int t = tid; t < 256; t += nthr) {
+                uint32_t sum = 0;
+                for (int w = 0; w < (nthr >> 5); w++) sum += S.hist[w * 256 + t];
+                S.tot[t] = sum;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                // 8 buckets per lane, lane-ordered
+                uint32_t loc[8];
+                uint32_t ls = 0;
+#pragma unroll
+                for (int u = 0; u < 8; u++) { loc[u] = S.tot[lane * 8 + u]; ls += loc[u]; }
+                uint32_t inc = ls;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t y = __shfl_up_sync(FULL_MASK, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                uint32_t before = inc - ls;
+                // the bucket where the running count first reaches rem
+                if ((int)before < rem && rem <= (int)inc) {
+                    uint32_t cum = before;
+                    for (int u = 0; u < 8; u++) {
+                        if ((int)(cum + loc[u]) >= rem) {
+                            S.misc[0] = lane * 8 + u;
+                            S.misc[1] = (int)cum;
+                            S.misc[2] = (int)loc[u];
+                            break;
+                        }
+                        cum += loc[u];
+                    }
+                }
+            }
+            __syncthreads();
+            const int dg = S.misc[0], cum = S.misc[1], cnt = S.misc[2];
+            rem -= cum;
+            prefix |= (unsigned long long)dg << shift;
+            pmask |= (unsigned long long)dm << shift;
+            __syncthreads();
+            if (cnt == rem) break;
+        }
+    }
+
+    // --- compact survivors ((key & pmask) <= prefix) into sortbuf ---
+    int nsurv = 0;
+    if (R > 0) {
+        if (REG) {
+            int cnt = 0;
+#pragma unroll
+            for (int q = 0; q < (REG ? KPT : 1); q++)
+                if (tid + q * nthr < V && (kr[q] & pmask) <= prefix) cnt++;
+            int tot;
+            int off = block_exclusive_scan(cnt, &tot, wsum);
+#pragma unroll
+            for (int q = 0; q < (REG ? KPT : 1); q++)
+                if (tid + q * nthr < V && (kr[q] & pmask) <= prefix && off < R) S.sortbuf[off++] = kr[q];
+            nsurv = tot;
+        } else {
+            int base = 0;
+            for (int i0 = 0; i0 < V; i0 += nthr) {
+                int idx = i0 + tid;
+                unsigned long long k = idx < V ? keys[idx] : ~0ull;
+                int f = (idx < V && (k & pmask) <= prefix) ? 1 : 0;
+                int tot;
+                int off = block_exclusive_scan(f, &tot, wsum);
+                if (f && base + off < R) S.sortbuf[base + off] = k;
+                base += tot;
+            }
+            nsurv = base;
+        }
+    }
+    if (nsurv != R) {
+        if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
+        nsurv = nsurv < R ? nsurv : R;
+    }
+
+    // --- bitonic sort of the survivors ---
+    if (R > 1) {
+        int ns = 1;
+        while (ns < R) ns <<= 1;
+        for (int t = R + tid; t < ns; t += nthr) S.sortbuf[t] = ~0ull;
+        __syncthreads();
+        for (int k = 2; k <= ns; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int pi = tid; pi < (ns >> 1); pi += nthr) {
+                    const int lo = ((pi & ~(j - 1)) << 1) | (pi & (j - 1));
+                    const int hi = lo + j;
+                    const bool up = (lo & k) == 0;
+                    unsigned long long x = S.sortbuf[lo], y = S.sortbuf[hi];
+                    if ((x > y) == up) { S.sortbuf[lo] = y; S.sortbuf[hi] = x; }
+                }
+                const int nj = (j > 1) ? (j >> 1) : (k << 1) >> 1;
+                if (j >= 64 || nj >= 64) __syncthreads(); else __syncwarp();
+            }
+        }
+        __syncthreads();
+    } else {
+        __syncthreads();
+    }
+    uint32_t* sel = a.sel + d.sel_off;
+    for (int r = tid; r < R; r += nthr) sel[r] = (uint32_t)(S.sortbuf[r] & 0xFFFFFFFFull);
+
+    // --- fillers: the lowest-numbered unscored slots (v1 / v2 only) ---
+    if (keff > R) {
+        const int F = keff - R;
+        const int W = d.words;
+        const uint32_t* mk = a.masks + d.mask_off;
+        int base = 0;
+        for (int c0 = 0; c0 < P && base < F; c0 += nthr) {
+            const int c = c0 + tid;
+            int f = 0;
+            if (c < P) {
+                int pc = 0;
+                for (int w = 0; w < W; w++) pc += __popc(mk[(int64_t)c * W + w]);
+                f = n - pc;
+            }
+            int tot;
+            const int off = block_exclusive_scan(f, &tot, wsum);
+            if (c < P && base + off < F) {
+                int out = R + base + off;
+                const int lim = F - base - off;
+                int got = 0;
+                for (int b = 0; b < n && got < lim && got < f; b++) {
+                    uint32_t word = mk[(int64_t)c * W + (b >> 5)];
+                    if (!((word >> (b & 31)) & 1u)) {
+                        sel[out + got] = kFillerFlag | (uint32_t)(c * n + b);
+                        got++;
+                    }
+                }
+            }
+            base += tot;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        st.P = keff;
+        st.V = 0;
+        st.materialized += keff;
+    }
+}
+
+__global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int seg = blockIdx.x;
+    const SegDesc& d = a.segs[seg];
+    if (d.mode > MODE_CLEAN || s >= d.N) return;
+    SegState& st = a.st[seg];
+    if (threadIdx.x == 0) {
+        st.expanded += st.V;
+        st.slots += (long long)st.P * d.n;
+        if (st.P > 0) st.levels += 1;
+    }
+    if (s == d.N - 1) return;  // the last level's sort and gather are not observable
+    __syncthreads();
+    if (st.V <= 16 * kSelectThreads) select_gpu<true>(d, st, a, s, smem);
+    else select_gpu<false>(d, st, a, s, smem);
+}
+
+// ------------------------------------------------------------------------------------
+// k_heap: ICH / PMS selection, serial per beam in the CPU solvers' order.  Thread 0
+// consumes the glibc rand() stream and runs the libstdc++ bounded-heap steps
+// (jssp_types.h:47-58) on shared memory; warp 1 stages the next parents' child tables.
+// ------------------------------------------------------------------------------------
+struct HeapSmem {
+    unsigned long long* hk;
+    uint32_t* hv;
+    uint32_t* ring;
+    uint8_t* stage;
+};
+
+// hk [K] u64 | hv [K] u32 | ring [64] u32 | misc [16] i32 | (16-aligned) stage [2][stage_bytes]
+__host__ __device__ __forceinline__ size_t heap_stage_offset(int k)
+{
+    return (((size_t)k * 12 + 64 * 4 + 16 * 4) + 15) & ~(size_t)15;
+}
+
+size_t heap_smem_bytes(int max_k, int stage_bytes)
+{
+    return heap_stage_offset(max_k) + 2 * (size_t)stage_bytes;
+}
+
+__device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* hv, int hole, int top,
+                                             unsigned long long vk, uint32_t vv)
+{
+    int parent = (hole - 1) / 2;
+    while (hole > top && hk[parent] < vk) {
+        hk[hole] = hk[parent];
+        hv[hole] = hv[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    hk[hole] = vk;
+    hv[hole] = vv;
+}
+
+__device__ void heap_adjust(unsigned long long* hk, uint32_t* hv, int hole, int len,
+                            unsigned long long vk, uint32_t vv)
+{
+    const int top = hole;
+    int child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (hk[child] < hk[child - 1]) child--;
+        hk[hole] = hk[child];
+        hv[hole] = hv[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        hk[hole] = hk[child - 1];
+        hv[hole] = hv[child - 1];
+        hole = child - 1;
+    }
+    heap_sift_up(hk, hv, hole, top, vk, vv);
+}
+
+// insert_into_beam (jssp_types.h:47-58) with push_heap / pop_heap semantics.
+__device__ __forceinline__ void heap_insert(unsigned long long* hk, uint32_t* hv, int& size, int K,
+                                            unsigned long long key, uint32_t val)
+{
+    if (size < K) {
+        hk[size] = key;
+        hv[size] = val;
+        size++;
+        heap_sift_up(hk, hv, size - 1, 0, key, val);
+    } else if (key < hk[0]) {
+        if (size > 1) heap_adjust(hk, hv, 0, size - 1, hk[size - 1], hv[size - 1]);
+        hk[size - 1] = key;
+        hv[size - 1] = val;
+        heap_sift_up(hk, hv, size - 1, 0, key, val);
+    }
+}
+
+struct Rng {
+    uint32_t* ring;
+    uint32_t i;
+    __device__ __forceinline__ uint32_t next()
+    {
+        uint32_t v = ring[(i - 31u) % 34u] + ring[(i - 3u) % 34u];
+        ring[i % 34u] = v;
+        i++;
+        return v >> 1;
+    }
+};
+
+__global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int seg = blockIdx.x;
+    const SegDesc& d = a.segs[seg];
+    if (d.mode < MODE_ICH || s >= d.N) return;
+    SegState& st = a.st[seg];
+    const int K = d.K, n = d.n, ab = d.auxbytes;
+    HeapSmem H;
+    H.hk = reinterpret_cast<unsigned long long*>(smem);
+    H.hv = reinterpret_cast<uint32_t*>(H.hk + K);
+    H.ring = H.hv + K;
+    int* hmisc = reinterpret_cast<int*>(H.ring + 64);
+    H.stage = smem + heap_stage_offset(K);
+    const int tid = threadIdx.x;
+    const int P = st.P;
+    const uint8_t* aux = a.aux_pool + d.aux_off;
+    if (tid < 34) H.ring[tid] = st.rng[tid];
+
+    // chunk 0 staged by everyone
+    const int nchunks = (P + chunk - 1) / chunk;
+    auto stage_chunk = [&](int q, int t0, int nt) {
+        if (q >= nchunks) return;
+        const int c0 = q * chunk;
+        const int cnt = (P - c0) < chunk ? (P - c0) : chunk;
+        const uint4* src = reinterpret_cast<const uint4*>(aux + (int64_t)c0 * ab);
+        uint4* dst = reinterpret_cast<uint4*>(H.stage + (size_t)(q & 1) * stage_bytes);
+        for (int u = t0; u < (cnt * ab) >> 4; u += nt) dst[u] = src[u];
+    };
+    stage_chunk(0, tid, blockDim.x);
+    __syncthreads();
+
+    int size = 0;
+    int best_cm = kSentinel;
+    uint32_t best_ref = 0;
+    long long gen = 0;
+    const int bound = st.bound;
+    const bool ich = (d.mode == MODE_ICH);
+    const bool last = (s == d.N - 1);
+    Rng g;
+    g.ring = H.ring;
+    g.i = st.rng_i;
+
+    for (int q = 0; q < nchunks; q++) {
+        if (tid >= 32) {
+            stage_chunk(q + 1, tid - 32, blockDim.x - 32);
+        } else if (tid == 0) {
+            const int c0 = q * chunk;
+            const int cend = (P - c0) < chunk ? P : c0 + chunk;
+            const uint8_t* sbuf = H.stage + (size_t)(q & 1) * stage_bytes;
+            for (int c = c0; c < cend; c++) {
+                const uint8_t* pa = sbuf + (size_t)(c - c0) * ab;
+                const int rc = (int)*reinterpret_cast<const uint32_t*>(pa);
+                const int32_t* cc = reinterpret_cast<const int32_t*>(pa + 4);
+                const uint8_t* cmv = pa + 4 + 4 * n;
+                const uint8_t* jb = pa + 4 + 5 * n;
+                if (ich) {
+                    // cpu/v0_ich/solver.cpp:24-39: score = cmax + (rand()%100)*0.01; the pair
+                    // (cmax, rand()%100) orders exactly like that double
+                    for (int i = 0; i < rc; i++) {
+                        const uint32_t dr = g.next();
+                        const unsigned long long key = (unsigned long long)cc[i] * 100ull + (dr % 100u);
+                        heap_insert(H.hk, H.hv, size, K, key, ((uint32_t)c << 8) | (uint32_t)i);
+                    }
+                    gen += rc;
+                } else if (rc > 0) {
+                    // cpu/v1_pms/solver.cpp:30-62
+                    const uint32_t dp = g.next();
+                    const int target = cmv[dp % (uint32_t)rc];
+                    for (int i = 0; i < rc; i++) {
+                        if (cmv[i] != target) continue;
+                        const uint32_t dn = g.next();
+                        const double sc = __dadd_rn(__ddiv_rn((double)cc[i], (double)(s + 1)),
+                                                    __ddiv_rn((double)(dn % 1000u), 1000000.0));
+                        gen++;
+                        if (last && cc[i] < best_cm) {
+                            best_cm = cc[i];
+                            best_ref = ((uint32_t)c << 8) | (uint32_t)jb[i];
+                        }
+                        if (cc[i] < bound)
+                            heap_insert(H.hk, H.hv, size, K, (unsigned long long)__double_as_longlong(sc),
+                                        ((uint32_t)c << 8) | (uint32_t)i);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    if (tid == 0) {
+        hmisc[0] = size;
+        st.rng_i = g.i;
+        st.expanded += gen;
+        st.slots += gen;
+        if (P > 0) st.levels += 1;
+        st.P = size;
+        if (!last) st.materialized += size;
+        if (last) {
+            if (ich) {
+                // min makespan over the final beam, first in array order (v0_ich :47-51)
+                for (int r = 0; r < size; r++) {
+                    const uint32_t e = H.hv[r];
+                    const int c = (int)(e >> 8), i = (int)(e & 0xFFu);
+                    const uint8_t* pa = aux + (int64_t)c * ab;
+                    const int cm = reinterpret_cast<const int32_t*>(pa + 4)[i];
+                    if (cm < best_cm) {
+                        best_cm = cm;
+                        best_ref = ((uint32_t)c << 8) | (uint32_t)pa[4 + 5 * n + i];
+                    }
+                }
+            }
+            st.best_cmax = best_cm;
+            st.best_ref = best_ref;
+        }
+    }
+    __syncthreads();
+    if (tid < 34) st.rng[tid] = H.ring[tid];
+    const int out_size = hmisc[0];
+    uint32_t* sel = a.sel + d.sel_off;
+    for (int r = tid; r < out_size; r += blockDim.x) sel[r] = H.hv[r];
+}
+
+// ------------------------------------------------------------------------------------
+// k_finalize: result makespan and the best schedule rebuilt from the level history.
+// ------------------------------------------------------------------------------------
+__global__ void k_finalize(StepArgs a)
+{
+    const int seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= a.nseg) return;
+    const SegDesc& d = a.segs[seg];
+    SegState& st = a.st[seg];
+    int32_t* seq = a.seq_pool + d.seq_off;
+    const int N = d.N;
+    bool found = false;
+    int mk = kSentinel;
+    int c = 0, job = 0;
+    if (d.mode <= MODE_CLEAN) {
+        mk = st.bound;
+        if (st.best != ~0ull) {
+            const int cm = (int)(st.best >> 32);
+            const uint32_t slot = (uint32_t)((st.best >> 8) & 0xFFFFFFull);
+            job = (int)(st.best & 0xFFull);
+            c = (int)(slot / (uint32_t)d.n);
+            found = true;
+            mk = cm < mk ? cm : mk;
+        }
+    } else {
+        mk = st.best_cmax;
+        if (st.best_cmax < kSentinel) {
+            found = true;
+            c = (int)(st.best_ref >> 8);
+            job = (int)(st.best_ref & 0xFFu);
+        }
+    }
+    if (found && (c >= d.K || job >= d.n)) {
+        found = false;
+        atomicOr(&st.status, kStatusBadLineage);
+    }
+    if (found) {
+        seq[N - 1] = job;
+        for (int t = N - 2; t >= 0; t--) {
+            const uint32_t e = a.hist[d.hist_off + (int64_t)t * d.K + c];
+            if (e == kMark || (int)(e >> 8) >= d.K || (int)(e & 0xFFu) >= d.n) {
+                found = false;
+                atomicOr(&st.status, kStatusBadLineage);
+                break;
+            }
+            seq[t] = (int)(e & 0xFFu);
+            c = (int)(e >> 8);
+        }
+    }
+    if (found) {
+        int cnt[kMaxJobs];
+        for (int j = 0; j < d.n; j++) cnt[j] = 0;
+        for (int t = 0; t < N; t++) {
+            const int j = seq[t];
+            seq[t] = j * d.m + cnt[j] + 1;
+            cnt[j]++;
+        }
+    } else {
+        for (int t = 0; t < N; t++) seq[t] = 0;
+    }
+    st.makespan = mk;
+    st.found = found ? 1 : 0;
+}
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+size_t step_smem_bytes(int sb_max) { return (size_t)kWarpsPerStepCta * 2 * sb_max; }
+
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)select_smem_bytes(sort_cap));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_heap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)heap_smem_bytes(max_k, stage_bytes));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)step_smem_bytes(sb_max));
+}
+
+cudaError_t launch_step(const StepArgs& a, int s, int grid, cudaStream_t stream)
+{
+    k_step<<<grid, kWarpsPerStepCta * 32, step_smem_bytes(a.sb_max), stream>>>(a, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream)
+{
+    k_gather_v1<<<grid, kWarpsPerStepCta * 32, 0, stream>>>(a, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream)
+{
+    k_select<<<a.nseg, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
+                        cudaStream_t stream)
+{
+    k_heap<<<a.nseg, kHeapThreads, heap_smem_bytes(max_k, stage_bytes), stream>>>(a, s, chunk, stage_bytes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream)
+{
+    k_finalize<<<(a.nseg + 127) / 128, 128, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace bsj

@@ -1,0 +1,46 @@
+// bsj_kernels.h -- launch interface between the host engine and the level kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bsj_device.cuh"
+
+namespace bsj {
+
+// Everything a level kernel needs, passed by value (fits the kernel parameter space).
+struct StepArgs {
+    const SegDesc* segs;
+    SegState* st;
+    const int32_t* rank_prefix;   // [nseg+1] prefix sums of K (flattened rank space)
+    int32_t nseg;
+    int32_t total_ranks;
+    int32_t sb_max;               // per-warp state buffer bytes (max sbytes)
+    int32_t pad0;
+    uint8_t* beam_pool;
+    uint8_t* slot_pool;
+    unsigned long long* keys;
+    uint32_t* sel;
+    uint32_t* masks;
+    uint32_t* hist;
+    uint8_t* aux_pool;
+    const uint32_t* ops;          // (duration << 8) | machine per op, per instance
+    int32_t* group_best;
+    int32_t* seq_pool;
+};
+
+// Grid / shared-memory sizing helpers.
+size_t step_smem_bytes(int sb_max);
+size_t select_smem_bytes(int sort_cap);
+size_t heap_smem_bytes(int max_k, int stage_bytes);
+
+// Launchers (asynchronous on `stream`).
+cudaError_t launch_step(const StepArgs& a, int s, int grid, cudaStream_t stream);
+cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream);
+cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream);
+cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
+                        cudaStream_t stream);
+cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream);
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max);
+
+}  // namespace bsj

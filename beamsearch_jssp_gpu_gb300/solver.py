@@ -1,0 +1,253 @@
+"""Python front end of the solver library, mirroring the reference's entry points.
+
+``run_gpu_beam_search_v1`` / ``run_gpu_beam_search_v2`` keep the reference's names,
+argument meaning and return value (gpu/v1/solver.cuh:6-12, gpu/v2_twophases/solver.cuh:
+6-12); ``beam_search_ich`` / ``beam_search_pms`` are the GPU forms of the CPU solvers
+(cpu/v0_ich/solver.h:6, cpu/v1_pms/solver.h:6) with the ``srand`` seed made explicit.
+Everything runs through libbsj.so's C ABI on the GPU; errors raise ``BsjError``.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _native as nat
+from .instance import JSSPInstance
+
+__all__ = ["Context", "Plan", "BeamSpec", "run_gpu_beam_search_v1", "run_gpu_beam_search_v2",
+           "beam_search_ich", "beam_search_pms", "solve", "solve_batch", "solve_iterations"]
+
+
+def _i32p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+@dataclass
+class BeamSpec:
+    """One beam of a batch (include/bsj.h ``bsj_beam``)."""
+
+    mode: str = "v2"
+    beam_width: int = 1024
+    best_known: int = nat.NO_BOUND
+    seed: int = 0
+    instance: int = 0
+    bound_group: int = -1
+
+    def to_c(self) -> nat.Beam:
+        if self.mode not in nat.MODES:
+            raise ValueError(f"unknown mode {self.mode!r}; one of {sorted(nat.MODES)}")
+        return nat.Beam(nat.MODES[self.mode], int(self.beam_width), int(self.best_known),
+                        int(self.seed) & 0xFFFFFFFF, int(self.instance), int(self.bound_group))
+
+
+class _InstanceArrays:
+    """Keeps the int32 arrays of a batch of instances alive for a C call."""
+
+    def __init__(self, instances):
+        self.arrays = []
+        self.c = (nat.Instance * len(instances))()
+        for k, inst in enumerate(instances):
+            if isinstance(inst, JSSPInstance):
+                mc, du = inst.machine, inst.duration
+            else:
+                mc, du = inst
+            mc = np.ascontiguousarray(mc, dtype=np.int32)
+            du = np.ascontiguousarray(du, dtype=np.int32)
+            if mc.ndim != 2 or mc.shape != du.shape:
+                raise ValueError("an instance is a pair of [n, m] int arrays (machine, duration)")
+            self.arrays.append((mc, du))
+            self.c[k] = nat.Instance(mc.shape[0], mc.shape[1], _i32p(mc), _i32p(du))
+        self.sizes = [a[0].shape for a in self.arrays]
+
+
+class Context:
+    """A solver context on one CUDA device (``bsj_create``)."""
+
+    def __init__(self, device: int = -1):
+        self.lib = nat.load()
+        h = ctypes.c_void_p()
+        st = self.lib.bsj_create(ctypes.byref(h), int(device))
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, f"bsj_create(device={device}) failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bsj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, self.lib.bsj_last_error(self.h).decode(errors="replace"))
+
+    def solve_batch(self, instances: Sequence, beams: Sequence[BeamSpec], stream: int = 0) -> List[dict]:
+        ia = _InstanceArrays(instances)
+        cb = (nat.Beam * len(beams))(*[b.to_c() for b in beams])
+        res = (nat.Result * len(beams))()
+        seqs = []
+        for k, b in enumerate(beams):
+            n, m = ia.sizes[b.instance] if 0 <= b.instance < len(ia.sizes) else (0, 0)
+            s = np.zeros(max(n * m, 1), dtype=np.int32)
+            seqs.append(s)
+            res[k].sequence = _i32p(s)
+        st = self.lib.bsj_solve_batch(self.h, len(ia.arrays), ia.c, len(beams), cb, res,
+                                      ctypes.c_void_p(stream) if stream else None)
+        self._check(st)
+        return [_result_dict(res[k], seqs[k]) for k in range(len(beams))]
+
+    def solve(self, machine, duration, mode: str = "v2", beam_width: int = 1024, seed: int = 0,
+              best_known: int = nat.NO_BOUND, stream: int = 0) -> dict:
+        return self.solve_batch([(machine, duration)],
+                                [BeamSpec(mode, beam_width, best_known, seed, 0, -1)], stream)[0]
+
+    def solve_iterations(self, machine, duration, mode: str, beam_width: int, seeds,
+                         initial_bound: int = nat.NO_BOUND, stream: int = 0):
+        """Multi-start passes with the bound carried between rounds; ``seeds`` is
+        [iterations, beams].  Returns (best makespan, best sequence)."""
+        ia = _InstanceArrays([(machine, duration)])
+        sd = np.ascontiguousarray(seeds, dtype=np.uint32)
+        if sd.ndim != 2:
+            raise ValueError("seeds must be [iterations, beams]")
+        best = ctypes.c_int32()
+        n, m = ia.sizes[0]
+        seq = np.zeros(n * m, dtype=np.int32)
+        st = self.lib.bsj_solve_iterations(self.h, ia.c, nat.MODES[mode], int(beam_width), sd.shape[1],
+                                           sd.shape[0], sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                           int(initial_bound), ctypes.byref(best), _i32p(seq),
+                                           ctypes.c_void_p(stream) if stream else None)
+        self._check(st)
+        return best.value, seq
+
+    def plan(self, instances: Sequence, beams: Sequence[BeamSpec]) -> "Plan":
+        return Plan(self, instances, beams)
+
+
+class Plan:
+    """A prepared batch (``bsj_plan_*``): inputs uploaded once, runs enqueued on a stream."""
+
+    def __init__(self, ctx: Context, instances: Sequence, beams: Sequence[BeamSpec]):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self._ia = _InstanceArrays(instances)
+        self.beams = list(beams)
+        cb = (nat.Beam * len(beams))(*[b.to_c() for b in beams])
+        h = ctypes.c_void_p()
+        ctx._check(self.lib.bsj_plan_create(ctx.h, len(self._ia.arrays), self._ia.c, len(beams), cb,
+                                            ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bsj_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, stream: int = 0):
+        self.ctx._check(self.lib.bsj_plan_run(self.h, ctypes.c_void_p(stream) if stream else None))
+
+    def results(self, with_sequence: bool = True) -> List[dict]:
+        res = (nat.Result * len(self.beams))()
+        seqs = []
+        for k, b in enumerate(self.beams):
+            n, m = self._ia.sizes[b.instance]
+            s = np.zeros(n * m, dtype=np.int32)
+            seqs.append(s)
+            if with_sequence:
+                res[k].sequence = _i32p(s)
+        self.ctx._check(self.lib.bsj_plan_results(self.h, res))
+        return [_result_dict(res[k], seqs[k] if with_sequence else None) for k in range(len(self.beams))]
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.bsj_plan_launches(self.h))
+
+    def stats(self):
+        b = ctypes.c_double()
+        e = ctypes.c_int64()
+        l = ctypes.c_int64()
+        self.ctx._check(self.lib.bsj_plan_stats(self.h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(l)))
+        return dict(step_bytes=b.value, expanded=e.value, step_launches=l.value)
+
+    def set_timing(self, on: bool):
+        self.ctx._check(self.lib.bsj_plan_set_timing(self.h, 1 if on else 0))
+
+    KERNELS = ("k_step", "k_select", "k_heap", "k_gather_v1", "k_finalize")
+
+    def kernel_ms(self) -> dict:
+        ms = (ctypes.c_float * 5)()
+        cnt = (ctypes.c_int64 * 5)()
+        self.ctx._check(self.lib.bsj_plan_kernel_ms(self.h, ms, cnt, 5))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNELS)}
+
+
+def _result_dict(r: nat.Result, seq) -> dict:
+    return dict(makespan=int(r.makespan), found=bool(r.found), seq=seq, expanded=int(r.expanded),
+                slots=int(r.slots), levels=int(r.levels), group_best=int(r.group_best))
+
+
+_default_ctx: Optional[Context] = None
+
+
+def _ctx() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(-1)
+    return _default_ctx
+
+
+def solve(machine, duration, mode="v2", beam_width=1024, seed=0, best_known=nat.NO_BOUND) -> dict:
+    return _ctx().solve(machine, duration, mode, beam_width, seed, best_known)
+
+
+def solve_batch(instances, beams) -> List[dict]:
+    return _ctx().solve_batch(instances, beams)
+
+
+def solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound=nat.NO_BOUND):
+    return _ctx().solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound)
+
+
+def _run_ref_style(mode: str, inst: JSSPInstance, beam_width: int, best_known: int, random_seed: int,
+                   out_best_sequence) -> int:
+    r = _ctx().solve(inst.machine, inst.duration, mode, beam_width, random_seed, best_known)
+    if out_best_sequence is not None and r["makespan"] < nat.NO_BOUND:
+        out_best_sequence[: len(r["seq"])] = r["seq"]
+    return r["makespan"]
+
+
+def run_gpu_beam_search_v1(inst: JSSPInstance, beam_width: int, best_known: int, random_seed: int,
+                           out_best_sequence=None) -> int:
+    """gpu/v1/solver.cuh:6-12: returns min(best_known, best complete makespan) and fills
+    ``out_best_sequence`` (a mutable sequence of >= n*m ints) when the result < 500000."""
+    return _run_ref_style("v1", inst, beam_width, best_known, random_seed, out_best_sequence)
+
+
+def run_gpu_beam_search_v2(inst: JSSPInstance, beam_width: int, best_known: int, random_seed: int,
+                           out_best_sequence=None) -> int:
+    """gpu/v2_twophases/solver.cuh:6-12, same contract as run_gpu_beam_search_v1."""
+    return _run_ref_style("v2", inst, beam_width, best_known, random_seed, out_best_sequence)
+
+
+def beam_search_ich(inst: JSSPInstance, beam_width: int, seed: int = 12345) -> int:
+    """cpu/v0_ich/solver.cpp:8-54 on the GPU, after ``srand(seed)`` (12345 in
+    cpu/v0_ich/main.cpp:39)."""
+    return _ctx().solve(inst.machine, inst.duration, "ich", beam_width, seed)["makespan"]
+
+
+def beam_search_pms(inst: JSSPInstance, beam_width: int, best_known: int, seed: int) -> int:
+    """cpu/v1_pms/solver.cpp:8-70 on the GPU, after ``srand(seed)``."""
+    return _ctx().solve(inst.machine, inst.duration, "pms", beam_width, seed, best_known)["makespan"]

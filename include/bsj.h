@@ -1,0 +1,143 @@
+/*
+ * bsj.h -- C ABI of the GB300 beam-search engine for the job-shop scheduling problem.
+ *
+ * Plain C types only (no C++, no torch): pointers, sizes, status codes.  Every call
+ * returns a bsj_status; no call exits the process.  Host pointers are borrowed for the
+ * duration of the call.  A context owns one device, one stream by default and its device
+ * memory; contexts are independent, so several may be used from different threads.
+ *
+ * Reference interfaces these entry points replace (paths within bensdz/BeamSearch_JSSP_GPU):
+ *   run_gpu_beam_search_v1   gpu/v1/solver.cuh:6-12, gpu/v1/solver.cu:178-298
+ *   run_gpu_beam_search_v2   gpu/v2_twophases/solver.cuh:6-12, gpu/v2_twophases/solver.cu:256-386
+ *   beam_search_ich          cpu/v0_ich/solver.h:6, cpu/v0_ich/solver.cpp:8-54
+ *   beam_search_pms          cpu/v1_pms/solver.h:6, cpu/v1_pms/solver.cpp:8-70
+ *   (the C++ drop-ins with the exact reference signatures are in bsj_solver.h)
+ */
+#ifndef BSJ_H
+#define BSJ_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BSJ_OK = 0,
+    BSJ_ERR_INVALID = 1,   /* malformed argument or instance */
+    BSJ_ERR_LIMIT = 2,     /* outside the supported sizes (see BSJ_MAX_*) */
+    BSJ_ERR_CUDA = 3,      /* CUDA runtime error; bsj_last_error() has the text */
+    BSJ_ERR_NOMEM = 4,     /* device or host allocation failed */
+    BSJ_ERR_DEVICE = 5     /* a kernel reported an inconsistent state */
+} bsj_status;
+
+/* Search mode of one beam. */
+typedef enum {
+    BSJ_MODE_V1 = 0,     /* gpu/v1 semantics bit for bit: pivot-machine branching, hash
+                            noise, fp32 score, stable order; unscored child slots keep the
+                            content of earlier levels (gpu/v1/solver.cu:37-39,73,120,261) */
+    BSJ_MODE_V2 = 1,     /* gpu/v2_twophases semantics bit for bit: unscored ranks keep the
+                            ping-pong buffer's old state (gpu/v2_twophases/solver.cu:191) */
+    BSJ_MODE_CLEAN = 2,  /* same branching, score and order; only scored children compete */
+    BSJ_MODE_ICH = 3,    /* cpu/v0_ich: all ready ops, glibc rand() noise, bounded heap */
+    BSJ_MODE_PMS = 4     /* cpu/v1_pms: pivot machine from glibc rand(), fp64 score, heap */
+} bsj_mode;
+
+#define BSJ_MAX_JOBS 128
+#define BSJ_MAX_MACHINES 64
+#define BSJ_MAX_OPS 8192
+#define BSJ_MAX_BEAM 16384
+#define BSJ_MAX_DURATION 16777215
+#define BSJ_NO_BOUND 500000   /* the callers' "no bound" value, gpu/v1/main.cu:57 */
+
+/* One instance: n jobs x m machines, job j's k-th op at [j*m + k]; machines 0-based
+   (the text format's values, instance_parser.cpp:69-73). Host memory. */
+typedef struct {
+    int32_t n;
+    int32_t m;
+    const int32_t *machine;
+    const int32_t *duration;
+} bsj_instance;
+
+/* One beam (one search pass). */
+typedef struct {
+    int32_t mode;          /* bsj_mode */
+    int32_t beam_width;    /* K, 1..BSJ_MAX_BEAM */
+    int32_t best_known;    /* pruning bound; BSJ_NO_BOUND for none */
+    uint32_t seed;         /* gpu modes: random_seed; ICH/PMS: the srand() seed */
+    int32_t instance;      /* index into the instance array of the batch */
+    int32_t bound_group;   /* beams with the same group share one device best-makespan
+                              word (atomicMin); -1 = a group of its own */
+} bsj_beam;
+
+typedef struct {
+    int32_t makespan;      /* the value the reference entry point returns for the mode */
+    int32_t found;         /* 1 if a complete schedule was recorded */
+    int32_t *sequence;     /* caller-owned [n*m] host buffer or NULL: 1-based op ids
+                              (op = job*m + step + 1) in dispatch order */
+    int64_t expanded;      /* children scored, summed over levels */
+    int64_t slots;         /* child slots considered (P*n for gpu modes) */
+    int32_t levels;        /* levels executed */
+    int32_t group_best;    /* final value of the beam's bound-group word */
+} bsj_result;
+
+typedef struct bsj_context bsj_context;
+typedef struct bsj_plan bsj_plan;
+
+/* Version string of the library. */
+const char *bsj_version(void);
+const char *bsj_status_string(bsj_status s);
+
+/* Context on CUDA device `device` (-1 = current device). */
+bsj_status bsj_create(bsj_context **out, int device);
+void bsj_destroy(bsj_context *ctx);
+/* Text of the last error on this context (valid until the next call). */
+const char *bsj_last_error(const bsj_context *ctx);
+
+/* One beam on one instance, synchronous: the C form of run_gpu_beam_search_v1/v2
+   (mode V1/V2), beam_search_ich (ICH) and beam_search_pms (PMS).  `stream` is a
+   cudaStream_t (NULL = the context's stream). */
+bsj_status bsj_solve(bsj_context *ctx, const bsj_instance *inst, const bsj_beam *beam,
+                     bsj_result *result, void *stream);
+
+/* Many beams over many instances in one set of launches (independent seeds, batched
+   instances of uneven size, mixed modes).  results[i] belongs to beams[i]. */
+bsj_status bsj_solve_batch(bsj_context *ctx, int num_instances, const bsj_instance *instances,
+                           int num_beams, const bsj_beam *beams, bsj_result *results,
+                           void *stream);
+
+/* Multi-start driver (gpu/v1/main.cu:62-71 with the MPI ranks as beams): `iterations`
+   rounds of `num_beams` beams; round i's beams use seeds[i*num_beams + b] and, as their
+   pruning bound, the best makespan of all earlier rounds (frozen per round).  Each
+   results entry holds that beam's last round; *best receives the overall best. */
+bsj_status bsj_solve_iterations(bsj_context *ctx, const bsj_instance *inst, int mode,
+                                int beam_width, int num_beams, int iterations,
+                                const uint32_t *seeds, int32_t initial_bound,
+                                int32_t *best, int32_t *best_sequence, void *stream);
+
+/* Plans: the split form of bsj_solve_batch used for device-resident timing.
+   bsj_plan_create uploads instances and sizes device memory; bsj_plan_run enqueues every
+   level on `stream` (asynchronous); bsj_plan_results waits and copies results out. */
+bsj_status bsj_plan_create(bsj_context *ctx, int num_instances, const bsj_instance *instances,
+                           int num_beams, const bsj_beam *beams, bsj_plan **out);
+bsj_status bsj_plan_run(bsj_plan *plan, void *stream);
+bsj_status bsj_plan_results(bsj_plan *plan, bsj_result *results);
+void bsj_plan_destroy(bsj_plan *plan);
+/* Kernel launches one bsj_plan_run enqueues. */
+int64_t bsj_plan_launches(const bsj_plan *plan);
+/* Algorithmic bytes of the last run's k_step launches -- per materialised survivor one
+   parent snapshot read, one child snapshot written, its 4 B survivor id and 4 B history
+   entry; 8 B per emitted candidate key -- with the run's expanded children and k_step
+   launch count. */
+bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, int64_t *expanded,
+                          int64_t *step_launches);
+/* When enabled, bsj_plan_run records CUDA events around every launch of each kernel
+   class; bsj_plan_kernel_ms returns total ms per class and launch counts for the last run:
+   index 0 k_step, 1 k_select, 2 k_heap, 3 k_gather_v1, 4 k_finalize. */
+bsj_status bsj_plan_set_timing(bsj_plan *plan, int enable);
+bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches, int count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

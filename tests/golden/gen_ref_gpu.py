@@ -1,0 +1,93 @@
+"""Generate golden vectors from the reference's own gpu kernels (run on a GPU machine).
+
+The reference kernels are compiled from their sources (gpu/v1/solver.cu,
+gpu/v2_twophases/solver.cu) into oracle/_ref/ref_gpu_v{1,2}.cubin by ``make -C oracle ref``
+where the reference tree exists; oracle/ref_gpu_harness.cpp drives them with the
+reference host loop.  Each case runs in a fresh process, twice, and must agree with
+itself.  Instances are the seeded synthetic generator's, so only (n, m, instance seed)
+is recorded.
+
+    python tests/golden/gen_ref_gpu.py OUT.json
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from beamsearch_jssp_gpu_gb300.instance import synthetic_instance, write_instance  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_build", "ref_gpu_harness")
+CUBIN = {v: os.path.join(ROOT, "oracle", "_ref", f"ref_gpu_{v}.cubin") for v in ("v1", "v2")}
+
+# (n, m, instance seed, K, search seeds, best_known list)
+CASES = [
+    (10, 5, 0, 64, [0, 1, 2, 12345], [500000]),
+    (10, 5, 1, 64, [7], [500000]),
+    (20, 15, 0, 256, [0, 1, 2, 3], [500000]),
+    (20, 15, 1, 1024, [0, 1], [500000]),
+    (20, 15, 2, 4096, [0], [500000]),
+    (20, 15, 3, 16384, [0], [500000]),
+    (6, 4, 5, 8, [3, 4], [500000]),
+    (3, 2, 6, 2, [1], [500000]),
+    (1, 1, 7, 4, [0], [500000]),
+    (5, 1, 8, 4, [0, 9], [500000]),
+    (1, 6, 9, 4, [2], [500000]),
+    (40, 5, 10, 128, [0, 5], [500000]),
+    (50, 20, 11, 256, [0], [500000]),
+    (100, 20, 12, 64, [1], [500000]),
+]
+# bounded runs: best_known = unbounded result + slack, and = unbounded result (pruned)
+BOUND_CASES = [(10, 5, 0, 64, [0, 1]), (20, 15, 0, 256, [0]), (8, 6, 13, 32, [4])]
+
+
+def run(mode: str, path: str, K: int, bk: int, seed: int) -> dict:
+    out = subprocess.run([HARNESS, mode, CUBIN[mode], path, str(K), str(bk), str(seed)],
+                         capture_output=True, text=True, check=True).stdout
+    return json.loads(out)
+
+
+def main(out_path: str) -> None:
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "gpu-harness"])
+    tmp = tempfile.mkdtemp()
+    records = []
+
+    def case(n, m, iseed, K, seed, bk):
+        mc, du = synthetic_instance(n, m, iseed)
+        path = os.path.join(tmp, f"i_{n}_{m}_{iseed}.txt")
+        write_instance(path, mc, du)
+        for mode in ("v1", "v2"):
+            a = run(mode, path, K, bk, seed)
+            b = run(mode, path, K, bk, seed)
+            records.append(dict(mode=mode, n=n, m=m, instance_seed=iseed, K=K, seed=seed,
+                                best_known=bk, makespan=a["makespan"], sequence=a["sequence"],
+                                self_consistent=(a == b)))
+            print(mode, n, m, iseed, K, seed, bk, a["makespan"], "ok" if a == b else "SELF-MISMATCH",
+                  flush=True)
+            if mode == "v1":
+                base = a["makespan"]
+        return base
+
+    for (n, m, iseed, K, seeds, bks) in CASES:
+        for seed in seeds:
+            for bk in bks:
+                case(n, m, iseed, K, seed, bk)
+    for (n, m, iseed, K, seeds) in BOUND_CASES:
+        for seed in seeds:
+            base = case(n, m, iseed, K, seed, 500000)
+            for bk in (base + 15, base, base - 10):
+                case(n, m, iseed, K, seed, bk)
+    with open(out_path, "w") as f:
+        json.dump(dict(generator="tests/golden/gen_ref_gpu.py",
+                       source="reference gpu/v1 and gpu/v2_twophases kernels, sm_103a, GB300",
+                       records=records), f, indent=0)
+    print("wrote", len(records), "records to", out_path)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "ref_gpu_golden.json"))

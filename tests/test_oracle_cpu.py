@@ -1,0 +1,109 @@
+"""The CPU oracle pinned against the reference (no GPU needed).
+
+* glibc rand() restatement == libc rand()
+* ICH / PMS restatements == the reference's own CPU solvers compiled from their sources
+  (oracle/_ref/libref_cpu.so; present where the reference tree is, skipped elsewhere)
+* gpu-mode restatements == the reference's gpu kernels (tests/golden/ref_gpu_golden.json,
+  produced on a GB300 by tests/golden/gen_ref_gpu.py)
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+from beamsearch_jssp_gpu_gb300.instance import synthetic_instance, write_instance
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_gpu_golden.json")
+needs_ref = pytest.mark.skipif(not O.ref_cpu_available(), reason="reference CPU build absent")
+
+
+@pytest.mark.parametrize("seed", [0, 1, 12345, 2**31 - 1, 2**31 + 5, 2**32 - 1])
+def test_glibc_rand_matches_libc(seed):
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(ctypes.c_uint(seed))
+    want = [libc.rand() for _ in range(3000)]
+    assert O.glibc_rand(seed, 3000).tolist() == want
+
+
+SIZES = [(10, 5, 64), (6, 4, 8), (15, 5, 100), (8, 8, 32), (5, 1, 4), (3, 2, 2), (1, 1, 3), (1, 5, 2), (12, 3, 1)]
+
+
+@needs_ref
+@pytest.mark.parametrize("n,m,K", SIZES)
+def test_oracle_ich_matches_reference(tmp_path, n, m, K):
+    for iseed in range(3):
+        mc, du = synthetic_instance(n, m, iseed)
+        path = str(tmp_path / f"i{iseed}.txt")
+        write_instance(path, mc, du)
+        for seed in (12345, iseed, 99 + iseed):
+            assert O.solve(mc, du, "ich", K, seed)["makespan"] == O.ref_ich(path, K, seed)
+
+
+@needs_ref
+@pytest.mark.parametrize("n,m,K", SIZES)
+def test_oracle_pms_matches_reference(tmp_path, n, m, K):
+    for iseed in range(3):
+        mc, du = synthetic_instance(n, m, iseed)
+        path = str(tmp_path / f"i{iseed}.txt")
+        write_instance(path, mc, du)
+        for seed in (0, 7 + iseed):
+            base = O.ref_pms(path, K, 500000, seed)
+            assert O.solve(mc, du, "pms", K, seed)["makespan"] == base
+            for bk in (base + 25, base, base - 5):
+                assert O.solve(mc, du, "pms", K, seed, best_known=bk)["makespan"] == O.ref_pms(path, K, bk, seed)
+
+
+@needs_ref
+def test_oracle_pms_larger_matches_reference(tmp_path):
+    mc, du = synthetic_instance(20, 15, 4)
+    path = str(tmp_path / "i.txt")
+    write_instance(path, mc, du)
+    for seed in (0, 1):
+        assert O.solve(mc, du, "pms", 256, seed)["makespan"] == O.ref_pms(path, 256, 500000, seed)
+
+
+@pytest.mark.parametrize("mode", ["ich", "pms", "v1", "v2", "clean"])
+def test_oracle_schedules_verify(mode):
+    for iseed in range(3):
+        mc, du = synthetic_instance(9, 4, iseed)
+        r = O.solve(mc, du, mode, 16, iseed)
+        assert r["found"]
+        assert O.schedule_makespan(mc, du, r["seq"]) == r["makespan"]
+
+
+def test_oracle_m1_reference_quirk():
+    """With m == 1 the reference reads op_finish[op-1] of the previous job
+    (jssp_types.h:82): jobs then run back to back even on different machines."""
+    mc = np.zeros((4, 1), dtype=np.int32)
+    du = np.array([[3], [5], [2], [4]], dtype=np.int32)
+    r = O.solve(mc, du, "v2", 8, 0)
+    assert r["makespan"] == 14
+
+
+def _golden():
+    if not os.path.exists(GOLDEN):
+        pytest.skip("reference gpu goldens not generated yet")
+    with open(GOLDEN) as f:
+        return json.load(f)["records"]
+
+
+def test_golden_self_consistent():
+    recs = _golden()
+    assert recs and all(r["self_consistent"] for r in recs)
+
+
+@pytest.mark.parametrize("mode", ["v1", "v2"])
+def test_oracle_gpu_modes_match_reference_kernels(mode):
+    """The gpu-mode restatement reproduces the reference gpu kernels' makespan, and the
+    sequence wherever the reference's best is unique (its copy is racy on ties)."""
+    recs = [r for r in _golden() if r["mode"] == mode and r["K"] <= 1024]
+    assert recs
+    for r in recs:
+        mc, du = synthetic_instance(r["n"], r["m"], r["instance_seed"])
+        got = O.solve(mc, du, mode, r["K"], r["seed"], best_known=r["best_known"])
+        assert got["makespan"] == r["makespan"], r
+        if r["makespan"] < 500000 and got["found"] and r["m"] > 1:
+            assert O.schedule_makespan(mc, du, r["sequence"]) == r["makespan"]
