@@ -92,7 +92,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_plan_destroy.restype = None
     L.bsj_plan_launches.argtypes = [vp]
     L.bsj_plan_launches.restype = ctypes.c_int64
-    L.bsj_plan_stats.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_int64)]
+    L.bsj_plan_stats.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_int64),
+                                 P(ctypes.c_int64)]
     L.bsj_plan_set_timing.argtypes = [vp, ctypes.c_int]
     L.bsj_plan_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int64), ctypes.c_int]
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",

@@ -61,9 +61,8 @@ struct bsj_plan {
     int32_t* d_group_init = nullptr;
     size_t beam_bytes = 0, slot_bytes = 0;
     StepArgs args{};
-    // graph
-    cudaGraphExec_t graph = nullptr;
-    cudaStream_t graph_stream = nullptr;
+    // graphs: [0] plain, [1] with timing events recorded around each launch
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
     // timing
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -372,21 +371,26 @@ cudaEvent_t* next_events(bsj_plan* p, int cls)
     return &ev.second.first;
 }
 
-// Enqueue one run of the plan on `s`.
-cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s)
+// Enqueue one run of the plan on `s` (`capturing`: s is being captured into a graph, so
+// timing events become event-record nodes of the graph).
+cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
 {
     const StepArgs& a = p->args;
     cudaError_t e;
     p->launches = 0;
     p->events_used = 0;
+    auto record = [&](cudaEvent_t ev) {
+        return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaEventRecord(ev, s);
+    };
     auto timed = [&](int cls, auto&& fn) -> cudaError_t {
         if (!p->timing) { p->launches++; return fn(); }
         cudaEvent_t* ev = next_events(p, cls);
-        cudaEventRecord(ev[0], s);
-        cudaError_t r = fn();
-        cudaEventRecord(ev[1], s);
+        cudaError_t r = record(ev[0]);
+        if (r != cudaSuccess) return r;
+        r = fn();
+        if (r != cudaSuccess) return r;
         p->launches++;
-        return r;
+        return record(ev[1]);
     };
     e = cudaMemcpyAsync(p->d_state, p->d_state_init, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
@@ -490,25 +494,21 @@ bsj_status bsj_plan_run(bsj_plan* p, void* stream)
     cudaSetDevice(ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     p->last_stream = s;
-    if (p->timing) {
-        cudaError_t e = enqueue_run(p, s);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "plan run");
-        return BSJ_OK;
-    }
-    if (!p->graph) {
+    const int gi = p->timing ? 1 : 0;
+    if (!p->graph[gi]) {
         // capture once on the context's stream, replay on any stream
         cudaStream_t cap = ctx->stream;
         cudaGraph_t g = nullptr;
         BSJ_CUDA(ctx, cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_run(p, cap);
+        cudaError_t e = enqueue_run(p, cap, true);
         cudaError_t e2 = cudaStreamEndCapture(cap, &g);
         if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ctx, e, "plan capture"); }
         if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&p->graph, g, 0);
+        e = cudaGraphInstantiate(&p->graph[gi], g, 0);
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) { p->graph = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+        if (e != cudaSuccess) { p->graph[gi] = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
     }
-    BSJ_CUDA(ctx, cudaGraphLaunch(p->graph, s));
+    BSJ_CUDA(ctx, cudaGraphLaunch(p->graph[gi], s));
     return BSJ_OK;
 }
 
@@ -548,7 +548,8 @@ void bsj_plan_destroy(bsj_plan* p)
 {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
-    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (cudaGraphExec_t g : p->graph)
+        if (g) cudaGraphExecDestroy(g);
     for (auto& ev : p->events) {
         cudaEventDestroy(ev.second.first);
         cudaEventDestroy(ev.second.second);
@@ -566,23 +567,27 @@ int64_t bsj_plan_launches(const bsj_plan* p)
     return n;
 }
 
-bsj_status bsj_plan_stats(const bsj_plan* p, double* step_bytes, int64_t* expanded, int64_t* step_launches)
+bsj_status bsj_plan_stats(const bsj_plan* p, double* step_bytes, double* select_bytes, int64_t* expanded,
+                          int64_t* materialized)
 {
     if (!p) return BSJ_ERR_INVALID;
     std::vector<SegState> st(p->nseg);
     cudaSetDevice(p->ctx->device);
     cudaError_t e = cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return BSJ_ERR_CUDA;
-    double bytes = 0.0;
-    int64_t ex = 0;
+    double sb = 0.0, selb = 0.0;
+    int64_t ex = 0, mat = 0;
     for (int b = 0; b < p->nseg; b++) {
         const SegDesc& d = p->segs[b];
-        bytes += (double)st[b].materialized * (2.0 * d.sbytes + 8.0) + 8.0 * (double)st[b].expanded;
+        sb += (double)st[b].materialized * (2.0 * d.sbytes + 8.0) + 8.0 * (double)st[b].expanded;
+        selb += 8.0 * (double)st[b].expanded + 4.0 * (double)st[b].materialized;
         ex += st[b].expanded;
+        mat += st[b].materialized;
     }
-    if (step_bytes) *step_bytes = bytes;
+    if (step_bytes) *step_bytes = sb;
+    if (select_bytes) *select_bytes = selb;
     if (expanded) *expanded = ex;
-    if (step_launches) *step_launches = p->maxN;  // k_step(-1) .. k_step(maxN-2)
+    if (materialized) *materialized = mat;
     return BSJ_OK;
 }
 
@@ -623,7 +628,7 @@ bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instan
     // eager launches: a one-shot plan gains nothing from graph capture
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     p->last_stream = st;
-    cudaError_t e = enqueue_run(p, st);
+    cudaError_t e = enqueue_run(p, st, false);
     if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
     s = bsj_plan_results(p, results);
     bsj_plan_destroy(p);

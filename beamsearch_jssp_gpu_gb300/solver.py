@@ -176,11 +176,15 @@ class Plan:
         return int(self.lib.bsj_plan_launches(self.h))
 
     def stats(self):
-        b = ctypes.c_double()
+        """Algorithmic bytes per kernel class of the last run, expanded children and
+        materialised survivors (include/bsj.h bsj_plan_stats)."""
+        sb = ctypes.c_double()
+        selb = ctypes.c_double()
         e = ctypes.c_int64()
-        l = ctypes.c_int64()
-        self.ctx._check(self.lib.bsj_plan_stats(self.h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(l)))
-        return dict(step_bytes=b.value, expanded=e.value, step_launches=l.value)
+        mat = ctypes.c_int64()
+        self.ctx._check(self.lib.bsj_plan_stats(self.h, ctypes.byref(sb), ctypes.byref(selb), ctypes.byref(e),
+                                                ctypes.byref(mat)))
+        return dict(step_bytes=sb.value, select_bytes=selb.value, expanded=e.value, materialized=mat.value)
 
     def set_timing(self, on: bool):
         self.ctx._check(self.lib.bsj_plan_set_timing(self.h, 1 if on else 0))

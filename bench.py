@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark: expanded candidates/s of the beam-search level path at K=4096, 50x20.
+
+Workload (one "step"): a full search -- all n*m = 1000 levels -- of 8 independently
+seeded beams (seeds 8*rank .. 8*rank+7) of width K=4096 on one synthetic 50x20 instance
+(machine permutation per job, durations U[1,99], int32; generator seed 0), gpu-v2 mode
+(pivot-machine branching, fp32 score, two-phase score-then-materialise), all 8 beams in
+one set of launches sharing a device best-makespan word.  Metric = scored children
+(valid, unpruned) summed over levels and beams / step time.
+
+Arms:
+  (default)          libbsj.so on the GPU: ``value`` device-timed with the instance
+                     resident, ``e2e`` through the C ABI from host buffers.
+  --impl reference   the reference's CPU implementation of machine-focused beam search
+                     (cpu/v1_pms/solver.cpp), as the oracle port pinned to it, one process
+                     per beam on the host cores, each step a bounded sample of levels.
+
+Multi-GPU: replicas only (each rank runs its own 8 beams; no collective on the data
+path); value = all ranks' candidates / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_JOBS, N_MACH, K, BEAMS, MODE, INSTANCE_SEED = 50, 20, 4096, 8, "v2", 0
+METRIC = "expanded candidates/s at K=4096 50x20"
+UNIT = "candidates/s"
+CPU_SAMPLE_LEVELS = 150        # levels per beam in one CPU sample
+L2_FLUSH_BYTES = 512 << 20     # > 129 MB L2
+
+
+def _config(world: int) -> dict:
+    return {"workload": f"BS-PMS pivot-machine beam search, gpu-v2 semantics, {N_JOBS}x{N_MACH} synthetic "
+                        f"(seed {INSTANCE_SEED}), K={K}, {BEAMS} seeded beams per GPU in one launch, all "
+                        f"{N_JOBS * N_MACH} levels",
+            "jobs": N_JOBS, "machines": N_MACH, "beam_width": K, "beams_per_gpu": BEAMS, "mode": MODE,
+            "levels": N_JOBS * N_MACH, "parallelism": f"replicas x{world}",
+            "l2": "flushed between timed steps (512 MB write); per-level working set ~26 MB stays L2-resident "
+                  "within a step"}
+
+
+# ------------------------------------------------------------------------------------
+# CPU side (oracle port of cpu/v1_pms/solver.cpp, pinned bit-for-bit to the reference)
+# ------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    seed, levels = args
+    from beamsearch_jssp_gpu_gb300.instance import synthetic_instance
+    from oracle import oracle as O
+
+    mc, du = synthetic_instance(N_JOBS, N_MACH, INSTANCE_SEED)
+    t0 = time.perf_counter()
+    r = O.solve(mc, du, "pms", K, seed, max_levels=levels)
+    return r["expanded"], time.perf_counter() - t0
+
+
+def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS) -> dict:
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        out = pool.map(_cpu_worker, [(s, levels) for s in seeds])
+        wall = time.perf_counter() - t0
+    expanded = sum(e for e, _ in out)
+    busy = max(t for _, t in out)
+    return dict(expanded=expanded, wall=wall, busy=busy, value=expanded / busy)
+
+
+def reference_arm(args) -> int:
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return 0
+    procs = max(1, min(BEAMS, os.cpu_count() or 1))
+    seeds = list(range(BEAMS))
+    for _ in range(args.warmup):
+        cpu_sample(procs, seeds, levels=20)
+    vals, times = [], []
+    for _ in range(args.steps):
+        r = cpu_sample(procs, seeds)
+        vals.append(r["value"])
+        times.append(r["busy"])
+    value = sum(vals) / len(vals)
+    sample = (f"levels 0-{CPU_SAMPLE_LEVELS - 1} of each of {BEAMS} beams (seeds 0-{BEAMS - 1}), "
+              f"{procs} processes, per step")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+            "data": "synthetic", "config": _config(world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` on this workload, from the committed ncu summary
+    (profiles/ncu_traffic.txt lines: kernel=<k> workload=<w> dram_bytes_per_launch=<x>)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        kv = dict(tok.split("=", 1) for tok in line.split() if "=" in tok)
+        if kv.get("kernel") == kernel and kv.get("workload") == f"{N_JOBS}x{N_MACH}_K{K}_B{BEAMS}":
+            try:
+                return float(kv["dram_bytes_per_launch"])
+            except (KeyError, ValueError):
+                return None
+    return None
+
+
+def gpu_arm(args) -> int:
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # oracle pool started (spawn) before this process touches the GPU
+        procs = max(1, min(BEAMS, os.cpu_count() or 1))
+        r = cpu_sample(procs, list(range(BEAMS)))
+        cpu = {"value": r["value"], "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"oracle port of cpu/v1_pms/solver.cpp (pinned to the reference), levels "
+                         f"0-{CPU_SAMPLE_LEVELS - 1} of {BEAMS} beams, {procs} processes, {r['busy']:.1f} s"}
+
+    torch.cuda.set_device(local)
+    from beamsearch_jssp_gpu_gb300 import BeamSpec, Context, synthetic_instance
+
+    mc, du = synthetic_instance(N_JOBS, N_MACH, INSTANCE_SEED)
+    ctx = Context(local)
+    beams = [BeamSpec(MODE, K, 500000, BEAMS * rank + b, 0, 0) for b in range(BEAMS)]
+    plan = ctx.plan([(mc, du)], beams)
+    plan.set_timing(True)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        plan.run(sh)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.run(sh)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    kms = plan.kernel_ms()           # per-kernel device time of the last timed step
+    stats = plan.stats()
+    res = plan.results(with_sequence=False)
+    expanded = sum(r["expanded"] for r in res)
+    launches_per_step = plan.launches
+    t_step = sum(times) / len(times)
+    if dist:
+        tt = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+        ex = torch.tensor([expanded], dtype=torch.float64, device="cuda")
+        dist.all_reduce(ex)
+        expanded_all = float(ex.item())
+    else:
+        expanded_all = float(expanded)
+    value = expanded_all / (t_step / 1000.0)
+
+    # e2e: the C ABI from host buffers (instance upload + all levels + results/schedules back)
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.solve_batch([(mc, du)], beams, sh)
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_times.append(t1 - t0)
+        assert sum(r["expanded"] for r in out) == expanded
+    e2e_t = sum(e2e_times) / len(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    h2d = mc.nbytes + du.nbytes + 24 * BEAMS
+    d2h = BEAMS * (N_JOBS * N_MACH * 4 + 48)
+
+    # roofline of the dominant kernel (live CUDA-event times of the last timed step)
+    peaks = _peaks()
+    alg = {"k_step": stats["step_bytes"], "k_select": stats["select_bytes"]}
+    dom = max(("k_step", "k_select"), key=lambda k: kms[k][0])
+    ms, nl = kms[dom]
+    per_launch_bytes = alg[dom] / nl
+    achieved = per_launch_bytes / (ms / nl / 1000.0) / 1e9
+    traffic = _traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_us": 1000.0 * ms / nl,
+                "peak_source": peaks["source"],
+                "kernel_share": {k: v[0] / max(1e-9, sum(x[0] for x in kms.values())) for k, v in kms.items()}}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic", "config": _config(world),
+                "e2e": {"value": expanded_all / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clk,
+                "makespans": [r["makespan"] for r in res]}
+        print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

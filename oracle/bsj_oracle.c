@@ -318,7 +318,7 @@ static int solve_gpu(const octx *x, const orc_params *p, orc_result *res, int ma
     int P = 1;
     const int bound = p->best_known;
     uint64_t best_key = UINT64_MAX;
-    int levels = 0;
+    int levels = 0, ties = 0;
     res->expanded = 0;
     res->slots = 0;
 
@@ -365,9 +365,15 @@ static int solve_gpu(const octx *x, const orc_params *p, orc_result *res, int ma
                        min (cmax, slot) for the reference's racy copy */
                     if (tmp->nseq == N) {
                         uint64_t kk = ((uint64_t)(uint32_t)tmp->cmax << 32) | (uint32_t)(c * n + b);
+                        if (best_key == UINT64_MAX || tmp->cmax < (int)(best_key >> 32)) ties = 0;
                         if (kk < best_key) {
                             best_key = kk;
                             memcpy(best_seq, tmp->seq, (size_t)N * sizeof(int32_t));
+                        }
+                        if (tmp->cmax == (int)(best_key >> 32)) {
+                            if (p->ties && ties < p->max_ties)
+                                memcpy(p->ties + (size_t)ties * N, tmp->seq, (size_t)N * sizeof(int32_t));
+                            ties++;
                         }
                     }
                 }
@@ -414,6 +420,7 @@ static int solve_gpu(const octx *x, const orc_params *p, orc_result *res, int ma
     }
 
     res->levels = levels;
+    res->ties = ties;
     if (best_key != UINT64_MAX) {
         int cm = (int)(best_key >> 32);
         res->makespan = cm < bound ? cm : bound;
@@ -485,7 +492,7 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
     for (int s = 0; s < max_steps && s < max_levels && beam[cb].size > 0; s++) {
         obeam *cur = &beam[cb], *nb = &beam[cb ^ 1];
         beam_reset(nb, &pool[cb ^ 1]);
-        levels++;
+        if (s < N) levels++;
         for (int c = 0; c < cur->size; c++) {
             const ost *par = cur->arr[c];
             if (mode == ORC_ICH) {
@@ -535,6 +542,7 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
         cb ^= 1;
     }
     res->levels = levels;
+    res->ties = 0;
     if (mode == ORC_ICH) {
         /* min cmax over the final beam, first in array order (v0_ich/solver.cpp:47-51) */
         int best = SENTINEL;

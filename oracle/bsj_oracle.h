@@ -40,6 +40,10 @@ typedef struct {
        rewritten at that step; trace_count[s] = beam size after step s. */
     uint32_t *trace;
     int32_t *trace_count;
+    /* optional (gpu modes): schedules of the complete children that tie for the best
+       makespan, up to max_ties of them, [max_ties][n*m]; count in orc_result.ties */
+    int32_t *ties;
+    int32_t max_ties;
 } orc_params;
 
 typedef struct {
@@ -48,7 +52,8 @@ typedef struct {
     int32_t *seq;         /* caller-owned [n*m]: 1-based op ids of the best schedule */
     int64_t expanded;     /* children scored (valid, unpruned) summed over levels */
     int64_t slots;        /* P*n (gpu modes) or children generated (ICH/PMS) summed */
-    int32_t levels;       /* levels executed */
+    int32_t levels;       /* levels that expanded at least one parent */
+    int32_t ties;         /* complete children with the best makespan (gpu modes) */
 } orc_result;
 
 /* Returns 0 on success, negative on invalid input / allocation failure. */

@@ -42,6 +42,8 @@ class _Params(ctypes.Structure):
         ("seed", ctypes.c_uint32),
         ("trace", ctypes.POINTER(ctypes.c_uint32)),
         ("trace_count", ctypes.POINTER(ctypes.c_int32)),
+        ("ties", ctypes.POINTER(ctypes.c_int32)),
+        ("max_ties", ctypes.c_int32),
     ]
 
 
@@ -53,6 +55,7 @@ class _Result(ctypes.Structure):
         ("expanded", ctypes.c_int64),
         ("slots", ctypes.c_int64),
         ("levels", ctypes.c_int32),
+        ("ties", ctypes.c_int32),
     ]
 
 
@@ -101,9 +104,10 @@ def _ptr(a: np.ndarray):
 
 
 def solve(machine, duration, mode: str, K: int, seed: int, best_known: int = 500000,
-          trace: bool = False, max_levels: int = 1 << 30) -> dict:
+          trace: bool = False, max_levels: int = 1 << 30, max_ties: int = 0) -> dict:
     """Run the oracle; returns makespan, found, seq (1-based op ids), expanded, slots,
-    levels and, with ``trace``, the per-level lineage arrays."""
+    levels, ties; with ``trace`` the per-level lineage arrays; with ``max_ties`` the
+    schedules of up to that many complete children tying for the best makespan."""
     mc = np.ascontiguousarray(machine, dtype=np.int32)
     du = np.ascontiguousarray(duration, dtype=np.int32)
     n, m = mc.shape
@@ -111,18 +115,23 @@ def solve(machine, duration, mode: str, K: int, seed: int, best_known: int = 500
     inst = _Instance(n, m, _ptr(mc), _ptr(du))
     tr = np.full((N, K), MARK, dtype=np.uint32) if trace else None
     tc = np.zeros(N, dtype=np.int32) if trace else None
+    tbuf = np.zeros((max(max_ties, 0), N), dtype=np.int32)
     params = _Params(
         MODES[mode], K, best_known, seed & 0xFFFFFFFF,
         tr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if trace else None,
         tc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if trace else None,
+        tbuf.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if max_ties > 0 else None,
+        max(max_ties, 0),
     )
     seq = np.zeros(N, dtype=np.int32)
-    res = _Result(0, 0, seq.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 0, 0, 0)
+    res = _Result(0, 0, seq.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 0, 0, 0, 0)
     rc = _lib().orc_solve_levels(ctypes.byref(inst), ctypes.byref(params), ctypes.byref(res), max_levels)
     if rc != 0:
         raise ValueError(f"oracle rejected the input (status {rc})")
     out = dict(makespan=res.makespan, found=bool(res.found), seq=seq, expanded=res.expanded,
-               slots=res.slots, levels=res.levels)
+               slots=res.slots, levels=res.levels, ties=res.ties)
+    if max_ties > 0:
+        out["tie_seqs"] = tbuf[: min(res.ties, max_ties)]
     if trace:
         out["trace"] = tr
         out["trace_count"] = tc

@@ -3,9 +3,10 @@
 The reference kernels are compiled from their sources (gpu/v1/solver.cu,
 gpu/v2_twophases/solver.cu) into oracle/_ref/ref_gpu_v{1,2}.cubin by ``make -C oracle ref``
 where the reference tree exists; oracle/ref_gpu_harness.cpp drives them with the
-reference host loop.  Each case runs in a fresh process, twice, and must agree with
-itself.  Instances are the seeded synthetic generator's, so only (n, m, instance seed)
-is recorded.
+reference host loop.  Each case runs in a fresh process, twice: the makespan must agree
+between the runs; the schedule may not, because several final-level threads copy into
+the best-solution buffer at once (gpu/v1/solver.cu:148-154, v2 :126-144).  Instances are
+the seeded synthetic generator's, so only (n, m, instance seed) is recorded.
 
     python tests/golden/gen_ref_gpu.py OUT.json
 """
@@ -66,9 +67,10 @@ def main(out_path: str) -> None:
             b = run(mode, path, K, bk, seed)
             records.append(dict(mode=mode, n=n, m=m, instance_seed=iseed, K=K, seed=seed,
                                 best_known=bk, makespan=a["makespan"], sequence=a["sequence"],
-                                self_consistent=(a == b)))
-            print(mode, n, m, iseed, K, seed, bk, a["makespan"], "ok" if a == b else "SELF-MISMATCH",
-                  flush=True)
+                                self_consistent=(a == b),
+                                makespan_consistent=(a["makespan"] == b["makespan"])))
+            print(mode, n, m, iseed, K, seed, bk, a["makespan"], b["makespan"],
+                  "same schedule" if a == b else "schedule differs between runs", flush=True)
             if mode == "v1":
                 base = a["makespan"]
         return base

@@ -22,21 +22,22 @@ def _records():
 
 @pytest.mark.parametrize("mode", ["v1", "v2"])
 def test_makespan_and_schedule_match_reference_kernels(ctx, mode):
+    """Makespan bit-exact against the reference kernels; the schedule equals the oracle's
+    deterministic choice, and the reference's own schedule is that one, another tie, or
+    a mix produced by its racy best-solution copy (gpu/v1/solver.cu:148-154)."""
     recs = [r for r in _records() if r["mode"] == mode]
     assert recs
     for r in recs:
         mc, du = synthetic_instance(r["n"], r["m"], r["instance_seed"])
         got = ctx.solve(mc, du, mode, r["K"], r["seed"], r["best_known"])
         assert got["makespan"] == r["makespan"], r
-        if r["makespan"] >= 500000:
-            continue
-        ref_seq = np.array(r["sequence"], dtype=np.int32)
-        if np.array_equal(got["seq"], ref_seq):
-            continue
-        # The reference copies its best schedule racily (gpu/v1/solver.cu:148-154): on a
-        # tie between complete children any of them may land.  A differing sequence is
-        # accepted only when it is a tie: same makespan, and the reference's sequence is
-        # itself one of the search's complete children with that makespan.
-        assert r["m"] > 1
-        assert O.schedule_makespan(mc, du, ref_seq) == r["makespan"]
-        assert O.schedule_makespan(mc, du, got["seq"]) == r["makespan"]
+        if r["K"] > 4096:
+            continue  # oracle too slow at this width; makespan parity only
+        want = O.solve(mc, du, mode, r["K"], r["seed"], best_known=r["best_known"], max_ties=4096)
+        assert np.array_equal(got["seq"], want["seq"])
+        if r["makespan"] < 500000:
+            ref = np.array(r["sequence"], dtype=np.int32)
+            explained = (np.array_equal(ref, got["seq"])
+                         or any(np.array_equal(ref, t) for t in want["tie_seqs"])
+                         or O.schedule_makespan(mc, du, ref) != r["makespan"])
+            assert explained, r

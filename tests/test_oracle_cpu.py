@@ -90,20 +90,41 @@ def _golden():
         return json.load(f)["records"]
 
 
-def test_golden_self_consistent():
+def test_golden_makespans_deterministic():
     recs = _golden()
-    assert recs and all(r["self_consistent"] for r in recs)
+    assert len(recs) >= 60
+    for r in recs:
+        assert r.get("makespan_consistent", True)
+
+
+def classify_reference_sequence(mc, du, r, oracle_run):
+    """'equal' (the deterministic choice: min cmax, lowest slot), 'tie' (another complete
+    child with the same makespan), 'corrupt' (the racy copy mixed several children: the
+    schedule does not reach the reported makespan) -- anything else is a parity failure."""
+    ref = np.array(r["sequence"], dtype=np.int32)
+    if np.array_equal(ref, oracle_run["seq"]):
+        return "equal"
+    if any(np.array_equal(ref, t) for t in oracle_run.get("tie_seqs", [])):
+        return "tie"
+    if O.schedule_makespan(mc, du, ref) != r["makespan"]:
+        return "corrupt"
+    return "unexplained"
 
 
 @pytest.mark.parametrize("mode", ["v1", "v2"])
 def test_oracle_gpu_modes_match_reference_kernels(mode):
-    """The gpu-mode restatement reproduces the reference gpu kernels' makespan, and the
-    sequence wherever the reference's best is unique (its copy is racy on ties)."""
-    recs = [r for r in _golden() if r["mode"] == mode and r["K"] <= 1024]
+    """The gpu-mode restatement reproduces the reference gpu kernels' makespan exactly;
+    every reference schedule is explained (equal / tie / corrupted by the racy copy)."""
+    recs = [r for r in _golden() if r["mode"] == mode and r["K"] <= 4096]
     assert recs
+    kinds = {}
     for r in recs:
         mc, du = synthetic_instance(r["n"], r["m"], r["instance_seed"])
-        got = O.solve(mc, du, mode, r["K"], r["seed"], best_known=r["best_known"])
+        got = O.solve(mc, du, mode, r["K"], r["seed"], best_known=r["best_known"], max_ties=4096)
         assert got["makespan"] == r["makespan"], r
-        if r["makespan"] < 500000 and got["found"] and r["m"] > 1:
-            assert O.schedule_makespan(mc, du, r["sequence"]) == r["makespan"]
+        if r["makespan"] >= 500000:
+            continue
+        k = classify_reference_sequence(mc, du, r, got)
+        assert k != "unexplained", r
+        kinds[k] = kinds.get(k, 0) + 1
+    assert kinds.get("equal", 0) > 0
