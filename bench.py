@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 N_JOBS, N_MACH, K, BEAMS, MODE, INSTANCE_SEED = 50, 20, 4096, 8, "v2", 0
 METRIC = "expanded candidates/s at K=4096 50x20"
 UNIT = "candidates/s"
-CPU_SAMPLE_LEVELS = 150        # levels per beam in one CPU sample
+CPU_SAMPLE_LEVELS = 1000       # levels per beam in one CPU sample (a full 50x20 search)
 L2_FLUSH_BYTES = 512 << 20     # > 129 MB L2
 
 
