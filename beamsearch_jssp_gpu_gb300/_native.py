@@ -24,7 +24,7 @@ EXPORTED = [
     "bsj_version", "bsj_status_string", "bsj_create", "bsj_destroy", "bsj_last_error",
     "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations", "bsj_plan_create", "bsj_plan_run",
     "bsj_plan_results", "bsj_plan_destroy", "bsj_plan_launches", "bsj_plan_stats",
-    "bsj_plan_set_timing", "bsj_plan_kernel_ms",
+    "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_solve_noalloc",
 ]
 
 
@@ -96,6 +96,10 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
                                  P(ctypes.c_int64)]
     L.bsj_plan_set_timing.argtypes = [vp, ctypes.c_int]
     L.bsj_plan_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int64), ctypes.c_int]
+    # allocation-free single-beam solve: device pointers in and out (include/bsj.h)
+    L.bsj_solve_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_int32, ctypes.c_uint32, vp, vp]
+    L.bsj_solve_noalloc.restype = ctypes.c_int
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
                  "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
                  "bsj_plan_set_timing", "bsj_plan_kernel_ms"):

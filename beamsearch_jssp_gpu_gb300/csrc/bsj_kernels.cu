@@ -998,6 +998,23 @@ cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_m
                                 (int)step_smem_bytes(sb_max));
 }
 
+template <typename F>
+static cudaError_t raise_smem(F* fn, size_t bytes)
+{
+    cudaFuncAttributes at;
+    cudaError_t e = cudaFuncGetAttributes(&at, fn);
+    if (e != cudaSuccess) return e;
+    if ((size_t)at.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t raise_kernel_smem(int sort_cap, int sb_max)
+{
+    cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
+    if (e != cudaSuccess) return e;
+    return raise_smem(k_step, step_smem_bytes(sb_max));
+}
+
 cudaError_t launch_step(const StepArgs& a, int s, int grid, cudaStream_t stream)
 {
     k_step<<<grid, kWarpsPerStepCta * 32, step_smem_bytes(a.sb_max), stream>>>(a, s);

@@ -42,5 +42,8 @@ cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stag
                         cudaStream_t stream);
 cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream);
 cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max);
+// Raise (never lower) the dynamic shared-memory limits of k_select and k_step to what
+// a launch with `sort_cap` / `sb_max` needs.
+cudaError_t raise_kernel_smem(int sort_cap, int sb_max);
 
 }  // namespace bsj

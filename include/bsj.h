@@ -137,6 +137,28 @@ bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, double *sele
 bsj_status bsj_plan_set_timing(bsj_plan *plan, int enable);
 bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches, int count);
 
+/* Single-beam solve that allocates nothing (no counterpart in the reference).
+   For callers that must not allocate device memory -- operator/plugin hosts whose device
+   memory is owned and budgeted by the host framework, and latency-critical loops where a
+   cudaMalloc/cudaFree would synchronise the device or could fail mid-run.  It needs no
+   context: all intermediate state lives in one library-owned scratch array of
+   BSJ_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit.
+     d_machine, d_duration  device [n*m] int32 (machines 0-based), read only
+     mode                   BSJ_MODE_V2 or BSJ_MODE_CLEAN
+     d_out                  device [2 + n*m] int32: makespan (-1 if the instance holds a
+                            machine id outside [0,m) or a duration outside [0,2^24)),
+                            found, then the 1-based op sequence
+   Asynchronous on `stream` (a cudaStream_t, NULL = default stream).  Returns
+   BSJ_ERR_LIMIT when n, m, beam_width exceed the BSJ_MAX_* limits or the beam's working
+   set (about 2*K*(4m+6n+16) + 8*K*n + 4*K*n*m bytes) exceeds the scratch array.  The
+   first call on each device looks up the scratch array's device address: make it before
+   any stream capture.  Calls share the scratch array: calls that overlap on one GPU race
+   and must be serialised by the caller. */
+#define BSJ_NOALLOC_SCRATCH_BYTES (64u << 20)
+bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t *d_machine,
+                             const int32_t *d_duration, int32_t mode, int32_t beam_width,
+                             int32_t best_known, uint32_t seed, int32_t *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
