@@ -93,7 +93,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_plan_launches.argtypes = [vp]
     L.bsj_plan_launches.restype = ctypes.c_int64
     L.bsj_plan_stats.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_int64),
-                                 P(ctypes.c_int64)]
+                                 P(ctypes.c_int64), P(ctypes.c_int64)]
     L.bsj_plan_set_timing.argtypes = [vp, ctypes.c_int]
     L.bsj_plan_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int64), ctypes.c_int]
     # allocation-free single-beam solve: device pointers in and out (include/bsj.h)

@@ -35,6 +35,9 @@ constexpr int kMaxBeam = 16384;
 constexpr int kMaxDuration = (1 << 24) - 1;
 constexpr int kSentinel = 500000;              // "no bound", gpu/v1/main.cu:57
 constexpr int kWarpsPerStepCta = 8;
+constexpr int kChunk = 32;                                 // ranks per k_step work unit
+constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;   // 4
+constexpr int kMaxChunks = kMaxBeam / kChunk;              // 512
 constexpr int kSelectThreads = 1024;
 constexpr int kHeapThreads = 64;
 
@@ -51,7 +54,9 @@ struct SegDesc {
     int32_t group;      // bound group
     int32_t auxbytes;   // per-parent bytes of the ICH/PMS child table
     int32_t op_off;     // index of this instance in the op table
-    int32_t pad0;
+    int32_t nq;         // ceil(n / 32): 32-lane groups a warp needs for the ready list
+    int32_t kcnt_off;   // index of this beam's first per-chunk key count
+    int32_t pad1;
     int64_t beam_off[2];  // byte offsets of the two beam buffers
     int64_t slot_off;     // byte offset of the v1 child-slot buffer
     int64_t key_off;      // u64 index: candidate keys of the current level
@@ -73,6 +78,7 @@ struct SegState {
     long long expanded;
     long long slots;
     long long materialized;   // survivors materialised (sum of beam sizes after each level)
+    long long select_fallbacks;  // levels whose top-K took the radix-select path
     int32_t levels;
     int32_t makespan;
     int32_t found;

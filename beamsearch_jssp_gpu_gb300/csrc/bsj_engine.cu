@@ -41,12 +41,16 @@ struct bsj_plan {
     int nseg = 0, ninst = 0, ngroups = 0;
     int maxN = 0;
     int total_ranks = 0;
+    int total_chunks = 0;
+    int nq_mask = 0;
+    int gather_grid = 1;
     int sort_cap = 0, heap_k = 0, heap_chunk = 1, heap_stage = 16;
     bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
     int step_grid = 1;
     std::vector<SegDesc> segs;
     std::vector<SegState> init;
     std::vector<int32_t> prefix;
+    std::vector<int32_t> cprefix;
     std::vector<int32_t> group_init;
     std::vector<int32_t> seg_group;
     // device
@@ -57,6 +61,7 @@ struct bsj_plan {
     SegState* d_state = nullptr;
     SegState* d_state_init = nullptr;
     int32_t* d_prefix = nullptr;
+    int32_t* d_cprefix = nullptr;
     int32_t* d_group = nullptr;
     int32_t* d_group_init = nullptr;
     size_t beam_bytes = 0, slot_bytes = 0;
@@ -189,10 +194,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     }
 
     // per-beam layout
-    size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0,
+    size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0, off_kcnt = 0,
            off_aux = 0, off_seq = 0;
-    int sb_max = 16, aux_max = 16;
+    int sb_max = 16, aux_max = 16, max_n = 1;
     p->prefix.push_back(0);
+    p->cprefix.push_back(0);
     for (int b = 0; b < nbeams; b++) {
         const bsj_beam& bm = beams[b];
         if (bm.instance < 0 || bm.instance >= ninst) { delete p; return fail(ctx, BSJ_ERR_INVALID, "beam: instance index out of range"); }
@@ -211,6 +217,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         d.auxbytes = (int)align_up((size_t)(4 + 6 * d.n), 16);
         d.group = gid[b];
         d.op_off = inst_off[bm.instance];
+        d.nq = nq_class(d.n);
+        p->nq_mask |= 1 << d.nq;
+        const int nch = (d.K + kChunk - 1) / kChunk;
+        d.kcnt_off = (int32_t)off_kcnt;
+        off_kcnt += nch;
         const size_t K = (size_t)d.K, n = (size_t)d.n, N = (size_t)d.N;
         const bool gpu = d.mode <= BSJ_MODE_CLEAN;
         const int nbuf = (d.mode == BSJ_MODE_V1) ? 1 : 2;
@@ -220,7 +231,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         d.slot_off = (int64_t)off_slot;
         if (d.mode == BSJ_MODE_V1) off_slot += align_up(K * n * d.sbytes, 256);
         d.key_off = (int64_t)off_keys;
-        if (gpu) off_keys += align_up(K * n, 32);
+        if (gpu) off_keys += align_up((size_t)nch * kChunk * n, 32);
         d.sel_off = (int64_t)off_sel;
         off_sel += align_up(K, 64);
         d.mask_off = (int64_t)off_mask;
@@ -233,7 +244,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         off_seq += align_up(N, 64);
         p->segs.push_back(d);
         p->prefix.push_back(p->prefix.back() + d.K);
+        p->cprefix.push_back(p->cprefix.back() + nch);
         sb_max = std::max(sb_max, d.sbytes);
+        max_n = std::max(max_n, d.n);
         aux_max = std::max(aux_max, d.auxbytes);
         p->maxN = std::max(p->maxN, d.N);
         if (d.mode == BSJ_MODE_V1) p->has_v1 = true;
@@ -253,6 +266,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         p->seg_group.push_back(gid[b]);
     }
     p->total_ranks = p->prefix.back();
+    p->total_chunks = p->cprefix.back();
     if (p->has_gpu) {
         int sc = 1;
         while (sc < p->sort_cap) sc <<= 1;
@@ -279,6 +293,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     const size_t o_state = take(sizeof(SegState) * nbeams);
     const size_t o_state_init = take(sizeof(SegState) * nbeams);
     const size_t o_prefix = take(sizeof(int32_t) * (nbeams + 1));
+    const size_t o_cprefix = take(sizeof(int32_t) * (nbeams + 1));
+    const size_t o_kcnt = take(sizeof(int32_t) * off_kcnt);
     const size_t o_group = take(sizeof(int32_t) * p->ngroups);
     const size_t o_group_init = take(sizeof(int32_t) * p->ngroups);
     const size_t o_ops = take(sizeof(uint32_t) * ops.size());
@@ -309,6 +325,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     p->d_state = reinterpret_cast<SegState*>(base + o_state);
     p->d_state_init = reinterpret_cast<SegState*>(base + o_state_init);
     p->d_prefix = reinterpret_cast<int32_t*>(base + o_prefix);
+    p->d_cprefix = reinterpret_cast<int32_t*>(base + o_cprefix);
     p->d_group = reinterpret_cast<int32_t*>(base + o_group);
     p->d_group_init = reinterpret_cast<int32_t*>(base + o_group_init);
 
@@ -318,7 +335,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.rank_prefix = p->d_prefix;
     a.nseg = nbeams;
     a.total_ranks = p->total_ranks;
+    a.chunk_prefix = p->d_cprefix;
+    a.total_chunks = p->total_chunks;
+    a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
     a.sb_max = sb_max;
+    a.max_n = max_n;
     a.beam_pool = base + o_beam;
     a.slot_pool = base + o_slot;
     a.keys = reinterpret_cast<unsigned long long*>(base + o_keys);
@@ -336,6 +357,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_segs, p->segs.data(), sizeof(SegDesc) * nbeams, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * nbeams, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_prefix, p->prefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_cprefix, p->cprefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_ops, ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -345,15 +367,17 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return cuda_fail(ctx, e, "plan upload");
     }
 
-    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16), sb_max);
+    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16), sb_max, max_n);
     if (e != cudaSuccess) {
         if (p->owns_mem) cudaFree(p->mem);
         delete p;
         return cuda_fail(ctx, e, "configure kernels");
     }
     // warps of k_step: one per rank, 8 per CTA, up to 8 CTAs per SM resident
+    // k_step: one CTA per chunk of kChunk ranks, at most 4 resident per SM
+    p->step_grid = std::max(1, std::min(p->total_chunks, ctx->sm_count * 4));
     int want = (p->total_ranks + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
-    p->step_grid = std::max(1, std::min(want, ctx->sm_count * 8));
+    p->gather_grid = std::max(1, std::min(want, ctx->sm_count * 8));
     *out = p;
     return BSJ_OK;
 }
@@ -403,7 +427,7 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
         if (p->slot_bytes) e = cudaMemsetAsync(a.slot_pool, 0, p->slot_bytes, s);
         if (e != cudaSuccess) return e;
     }
-    e = timed(0, [&] { return launch_step(a, -1, p->step_grid, s); });
+    e = timed(0, [&] { return launch_step(a, -1, p->step_grid, p->nq_mask, s); });
     if (e != cudaSuccess) return e;
     for (int lv = 0; lv < p->maxN; lv++) {
         if (p->has_gpu) {
@@ -416,10 +440,10 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
         }
         if (lv < p->maxN - 1) {
             if (p->has_v1) {
-                e = timed(3, [&] { return launch_gather_v1(a, lv, p->step_grid, s); });
+                e = timed(3, [&] { return launch_gather_v1(a, lv, p->gather_grid, s); });
                 if (e != cudaSuccess) return e;
             }
-            e = timed(0, [&] { return launch_step(a, lv, p->step_grid, s); });
+            e = timed(0, [&] { return launch_step(a, lv, p->step_grid, p->nq_mask, s); });
             if (e != cudaSuccess) return e;
         }
     }
@@ -568,7 +592,7 @@ int64_t bsj_plan_launches(const bsj_plan* p)
 }
 
 bsj_status bsj_plan_stats(const bsj_plan* p, double* step_bytes, double* select_bytes, int64_t* expanded,
-                          int64_t* materialized)
+                          int64_t* materialized, int64_t* select_fallbacks)
 {
     if (!p) return BSJ_ERR_INVALID;
     std::vector<SegState> st(p->nseg);
@@ -576,14 +600,16 @@ bsj_status bsj_plan_stats(const bsj_plan* p, double* step_bytes, double* select_
     cudaError_t e = cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return BSJ_ERR_CUDA;
     double sb = 0.0, selb = 0.0;
-    int64_t ex = 0, mat = 0;
+    int64_t ex = 0, mat = 0, fb = 0;
     for (int b = 0; b < p->nseg; b++) {
         const SegDesc& d = p->segs[b];
         sb += (double)st[b].materialized * (2.0 * d.sbytes + 8.0) + 8.0 * (double)st[b].expanded;
         selb += 8.0 * (double)st[b].expanded + 4.0 * (double)st[b].materialized;
         ex += st[b].expanded;
         mat += st[b].materialized;
+        fb += st[b].select_fallbacks;
     }
+    if (select_fallbacks) *select_fallbacks = fb;
     if (step_bytes) *step_bytes = sb;
     if (select_bytes) *select_bytes = selb;
     if (expanded) *expanded = ex;

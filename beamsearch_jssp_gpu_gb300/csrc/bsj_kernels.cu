@@ -37,6 +37,20 @@ __device__ __forceinline__ uint32_t op_info(const uint32_t* ops, int op_off, int
     return __ldg(ops + op_off + j * m + k);
 }
 
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Warp-wide asynchronous copy of one snapshot into shared memory (16-byte pieces).
+__device__ __forceinline__ void warp_prefetch(uint8_t* dst_smem, const uint8_t* src_gmem, int sbytes, int lane)
+{
+    for (int q = lane; q < (sbytes >> 4); q += 32) cp_async16(dst_smem + 16 * q, src_gmem + 16 * q);
+}
+
 // Root state: first op of every job ready in job order (gpu_snapshot.cuh:34-44,
 // jssp_types.h:61-72).
 __device__ void build_root(uint8_t* sb, const Lay& L, int lane)
@@ -55,18 +69,20 @@ __device__ void build_root(uint8_t* sb, const Lay& L, int lane)
     __syncwarp();
 }
 
-// Ready ops of the state in `sb`, lane-major: position i = lane + 32*q.
+// Ready ops of the state in `sb`, lane-major: position i = lane + 32*q, q < NQ = ceil(n/32).
+template <int NQ>
 struct ReadyOps {
     int r;
-    int job[4], k[4], mc[4], du[4];
+    int job[NQ], k[NQ], mc[NQ], du[NQ];
 };
 
+template <int NQ>
 __device__ __forceinline__ void load_ready(uint8_t* sb, const Lay& L, const uint32_t* ops,
-                                           int op_off, int lane, ReadyOps& R)
+                                           int op_off, int lane, ReadyOps<NQ>& R)
 {
     R.r = *H_R(sb, L);
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < NQ; q++) {
         int i = lane + 32 * q;
         R.mc[q] = -1;
         R.job[q] = 0;
@@ -88,30 +104,34 @@ __device__ __forceinline__ void load_ready(uint8_t* sb, const Lay& L, const uint
 // hashes (seed + rank), takes that ready op's machine, and lists the ready ops on that
 // machine in ready-list order; here every lane tests its ops and a ballot gives each
 // candidate its branch index b.
+template <int NQ>
 struct Cands {
-    unsigned bal[4];
-    int bidx[4];
+    unsigned bal[NQ];
+    int bidx[NQ];
     int cnt;
     int pm;
 };
 
-__device__ __forceinline__ void pivot_candidates(const ReadyOps& R, uint32_t seed_t, uint32_t c,
-                                                 int lane, Cands& C)
+template <int NQ>
+__device__ __forceinline__ void pivot_candidates(const ReadyOps<NQ>& R, uint32_t seed_t, uint32_t c,
+                                                 int lane, Cands<NQ>& C)
 {
     C.cnt = 0;
     C.pm = -1;
 #pragma unroll
-    for (int q = 0; q < 4; q++) { C.bal[q] = 0; C.bidx[q] = 0; }
+    for (int q = 0; q < NQ; q++) { C.bal[q] = 0; C.bidx[q] = 0; }
     if (R.r <= 0) return;
     uint32_t h = pivot_hash(seed_t + c);
     int pp = (int)(h % (uint32_t)R.r);
     int qp = pp >> 5;
-    int mine = (qp == 0) ? R.mc[0] : (qp == 1) ? R.mc[1] : (qp == 2) ? R.mc[2] : R.mc[3];
+    int mine = R.mc[0];
+#pragma unroll
+    for (int q = 1; q < NQ; q++) if (qp == q) mine = R.mc[q];
     int pm = __shfl_sync(FULL_MASK, mine, pp & 31);
     unsigned lt = (1u << lane) - 1u;
     int acc = 0;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < NQ; q++) {
         C.bal[q] = __ballot_sync(FULL_MASK, (lane + 32 * q < R.r) && R.mc[q] == pm);
         C.bidx[q] = acc + __popc(C.bal[q] & lt);
         acc += __popc(C.bal[q]);
@@ -133,6 +153,7 @@ __device__ __forceinline__ int pred_finish(uint8_t* sb, const Lay& L, int j, int
 // removal from the ready list (swap-with-last for the gpu modes, gpu/v1/solver.cu:100-106;
 // order-preserving erase for ICH/PMS, cpu/v0_ich/solver.cpp:29, cpu/v1_pms/solver.cpp:44-46),
 // then dev_schedule_operation (gpu_snapshot.cuh:47-70) and the makespan.
+template <int NQ>
 __device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int op_off, int i,
                             bool erase, uint32_t lineage, uint32_t stamp, int lane)
 {
@@ -146,15 +167,15 @@ __device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int o
     const int fin = (tr > pred ? tr : pred) + (int)(o >> 8);
     __syncwarp();
     if (erase) {
-        uint8_t v[4];
+        uint8_t v[NQ];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < NQ; q++) {
             int t = lane + 32 * q;
             v[q] = (t >= i && t < r - 1) ? RD(b, L)[t + 1] : 0;
         }
         __syncwarp();
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < NQ; q++) {
             int t = lane + 32 * q;
             if (t >= i && t < r - 1) RD(b, L)[t] = v[q];
         }
@@ -181,27 +202,31 @@ __device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int o
 // Expansion of one state for level t (gpu modes): kernel_expand_beam_layer /
 // kernel_score_candidates (gpu/v1/solver.cu:72-127, v2 :68-123) without the per-thread
 // snapshot copy -- a child's makespan needs only tr[pivot machine], the job's
-// predecessor finish and the parent makespan.
+// predecessor finish and the parent makespan.  Keys go to this CTA's chunk region at
+// positions reserved with a shared-memory counter.
 // ------------------------------------------------------------------------------------
-__device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc& d,
-                           SegState& st, const StepArgs& a, int c, int t, int lane)
+template <int NQ>
+__device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc& d, SegState& st,
+                           const StepArgs& a, int c, int t, int lane, unsigned long long* kstage,
+                           int* nv_out, const float* s_noise)
 {
-    ReadyOps R;
-    load_ready(sb, L, a.ops, d.op_off, lane, R);
+    ReadyOps<NQ> R;
+    load_ready<NQ>(sb, L, a.ops, d.op_off, lane, R);
     const uint32_t seed_t = d.seed + (uint32_t)t;
-    Cands C;
-    pivot_candidates(R, seed_t, (uint32_t)c, lane, C);
+    Cands<NQ> C;
+    pivot_candidates<NQ>(R, seed_t, (uint32_t)c, lane, C);
     const int ns1 = *H_NS(sb, L) + 1;
     const int pcmax = *H_CMAX(sb, L);
     const int bound = st.bound;
     const int trp = (C.pm >= 0) ? TR(sb)[C.pm] : 0;
     const bool last = (t == d.N - 1);
+    const float fns = __int2float_rn(ns1);
 
-    unsigned long long key[4];
-    unsigned vb[4];
+    unsigned long long key[NQ];
+    unsigned vb[NQ];
     uint32_t wacc[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < NQ; q++) {
         bool valid = false;
         key[q] = 0ull;
         if ((C.bal[q] >> lane) & 1u) {
@@ -211,7 +236,10 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
             valid = cm < bound;   // gpu/v1/solver.cu:120
             if (valid) {
                 const int b = C.bidx[q];
-                const float sc = gpu_score(cm, ns1, seed_t, (uint32_t)c, (uint32_t)b);
+                // (float)cmax / (float)ns + (float)(h % 1000) / 1e9f, IEEE round-to-nearest;
+                // the second quotient comes from a table of its 1000 possible values
+                const float base = __fdiv_rn(__int2float_rn(cm), fns);
+                const float sc = __fadd_rn(base, s_noise[noise_hash(seed_t, (uint32_t)c, (uint32_t)b) % 1000u]);
                 const uint32_t slot = (uint32_t)(c * L.n + b);
                 key[q] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
                 wacc[b >> 5] |= 1u << (b & 31);
@@ -224,27 +252,32 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
         }
         vb[q] = __ballot_sync(FULL_MASK, valid);
     }
-    int nv = __popc(vb[0]) + __popc(vb[1]) + __popc(vb[2]) + __popc(vb[3]);
-    int base = 0;
-    if (lane == 0 && nv > 0) base = atomicAdd(&st.V, nv);
-    base = __shfl_sync(FULL_MASK, base, 0);
+    int nv = 0;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) nv += __popc(vb[q]);
+    // keys of this parent in branch order: position among the valid ones = popc below,
+    // and branch order == ready-list order == lane-major order here
     const unsigned lt = (1u << lane) - 1u;
     int acc = 0;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        if ((vb[q] >> lane) & 1u) a.keys[d.key_off + base + acc + __popc(vb[q] & lt)] = key[q];
+    for (int q = 0; q < NQ; q++) {
+        if ((vb[q] >> lane) & 1u) kstage[acc + __popc(vb[q] & lt)] = key[q];
         acc += __popc(vb[q]);
     }
-    for (int w = 0; w < d.words; w++) {
-        uint32_t word = __reduce_or_sync(FULL_MASK, wacc[w & 3]);
-        if (lane == 0) a.masks[d.mask_off + (int64_t)c * d.words + w] = word;
+    if (lane == 0) *nv_out = nv;
+#pragma unroll
+    for (int w = 0; w < NQ; w++) {
+        if (w < d.words) {
+            uint32_t word = __reduce_or_sync(FULL_MASK, wacc[w]);
+            if (lane == 0) a.masks[d.mask_off + (int64_t)c * d.words + w] = word;
+        }
     }
 
     if (d.mode == MODE_V1 && nv > 0) {
         // kernel_expand_beam_layer also writes every scored child's snapshot into its
         // slot c*n+b (gpu/v1/solver.cu:129-145); slots it skips keep older content.
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < NQ; q++) {
             unsigned bits = vb[q];
             while (bits) {
                 const int l = __ffs(bits) - 1;
@@ -254,8 +287,8 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
                 const int j = __shfl_sync(FULL_MASK, R.job[q], l);
                 warp_copy_smem(cb, sb, L.sbytes, lane);
                 __syncwarp();
-                apply_child(cb, L, a.ops, d.op_off, i, false, ((uint32_t)c << 8) | (uint32_t)j,
-                            (uint32_t)(t + 1), lane);
+                apply_child<NQ>(cb, L, a.ops, d.op_off, i, false, ((uint32_t)c << 8) | (uint32_t)j,
+                                (uint32_t)(t + 1), lane);
                 warp_store(a.slot_pool + d.slot_off + (int64_t)(c * L.n + b) * L.sbytes, cb, L.sbytes, lane);
                 __syncwarp();
             }
@@ -266,18 +299,19 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
 // ICH / PMS: per ready position, the child's makespan, machine and job; the ordered
 // serial part (rand() draws, heap) runs in k_heap (cpu/v0_ich/solver.cpp:22-39,
 // cpu/v1_pms/solver.cpp:26-62).
+template <int NQ>
 __device__ void expand_compat(uint8_t* sb, const Lay& L, const SegDesc& d, const StepArgs& a,
                               int c, int lane)
 {
-    ReadyOps R;
-    load_ready(sb, L, a.ops, d.op_off, lane, R);
+    ReadyOps<NQ> R;
+    load_ready<NQ>(sb, L, a.ops, d.op_off, lane, R);
     const int pcmax = *H_CMAX(sb, L);
     uint8_t* base = a.aux_pool + d.aux_off + (int64_t)c * d.auxbytes;
     int32_t* cc = reinterpret_cast<int32_t*>(base + 4);
     uint8_t* cmv = base + 4 + 4 * L.n;
     uint8_t* jb = base + 4 + 5 * L.n;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < NQ; q++) {
         int i = lane + 32 * q;
         if (i < R.r) {
             const int pred = pred_finish(sb, L, R.job[q], R.k[q]);
@@ -292,91 +326,147 @@ __device__ void expand_compat(uint8_t* sb, const Lay& L, const SegDesc& d, const
 }
 
 // ------------------------------------------------------------------------------------
-// k_step: materialise level s+1 (warp per survivor) and expand it.
+// k_step: materialise level s+1 and expand it.  Work unit: a chunk of kChunk consecutive
+// ranks of one beam per CTA (kRanksPerWarp per warp).  Each warp first fetches the
+// selection entries of its ranks, then starts asynchronous copies of all their source
+// snapshots into shared memory, then materialises and expands them one after the other,
+// so the copies of later ranks overlap the work on earlier ones.  NQ = ceil(n/32).
 // ------------------------------------------------------------------------------------
+template <int NQ>
 __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int s)
 {
     extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ float s_noise[1000];
+    __shared__ int s_nv[kChunk], s_pre[kChunk], s_kcnt, s_P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint8_t* sb = smem + (size_t)warp * 2 * a.sb_max;
-    uint8_t* cb = sb + a.sb_max;
-    const int nw = gridDim.x * kWarpsPerStepCta;
-    for (int flat = blockIdx.x * kWarpsPerStepCta + warp; flat < a.total_ranks; flat += nw) {
-        const int seg = find_seg(a.rank_prefix, a.nseg, flat);
+    uint8_t* wbuf = smem + (size_t)warp * (kRanksPerWarp + 1) * a.sb_max;
+    uint8_t* cb = wbuf + (size_t)kRanksPerWarp * a.sb_max;
+    // candidate keys of the chunk's ranks, staged per rank (n slots each) so that they
+    // leave in slot order: ranks ascending, branches ascending
+    unsigned long long* kstage = reinterpret_cast<unsigned long long*>(
+        smem + (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * a.sb_max);
+    for (int k = threadIdx.x; k < 1000; k += blockDim.x)
+        s_noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
+    for (int chunk = blockIdx.x; chunk < a.total_chunks; chunk += gridDim.x) {
+        const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
         const SegDesc& d = a.segs[seg];
-        if (s >= d.N - 1) continue;
+        if (d.nq != NQ || s >= d.N - 1) continue;
         SegState& st = a.st[seg];
-        const int r = flat - __ldg(a.rank_prefix + seg);
-        const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
-        if (r >= P) continue;
+        const int q = chunk - __ldg(a.chunk_prefix + seg);
+        if (threadIdx.x == 0) s_P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
+        if (threadIdx.x < kChunk) s_nv[threadIdx.x] = 0;
+        __syncthreads();
+        const int P = s_P;
         const Lay L(d);
         const int mode = d.mode;
-        if (mode == MODE_V1) {
-            uint8_t* beam = a.beam_pool + d.beam_off[0];
+        const bool compat = (mode == MODE_ICH || mode == MODE_PMS);
+        const int r0 = q * kChunk + warp;
+        uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
+        const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
+        if (mode == MODE_V1) childbuf = a.beam_pool + d.beam_off[0];
+
+        // selection entries of this warp's ranks (one lane each)
+        uint32_t my_e = 0;
+        if (lane < kRanksPerWarp && s >= 0) {
+            const int r = r0 + lane * kWarpsPerStepCta;
+            if (r < P && mode != MODE_V1) my_e = __ldg(a.sel + d.sel_off + r);
+        }
+        // start all source copies
+#pragma unroll
+        for (int i = 0; i < kRanksPerWarp; i++) {
+            const int r = r0 + i * kWarpsPerStepCta;
+            const uint32_t e = __shfl_sync(FULL_MASK, my_e, i);
+            if (r >= P || s < 0) continue;
+            const uint8_t* src;
+            if (mode == MODE_V1) src = childbuf + (int64_t)r * L.sbytes;
+            else if (compat) src = parent + (int64_t)(e >> 8) * L.sbytes;
+            else src = parent + (int64_t)((e & ~kFillerFlag) / (uint32_t)L.n) * L.sbytes;
+            warp_prefetch(wbuf + (size_t)i * a.sb_max, src, L.sbytes, lane);
+        }
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncwarp();
+
+        unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * kChunk * L.n;
+        const int nst = L.n;  // staged keys per rank
+        uint32_t* hrow = a.hist + d.hist_off + (int64_t)(s < 0 ? 0 : s) * d.K;
+#pragma unroll 1
+        for (int i = 0; i < kRanksPerWarp; i++) {
+            const int r = r0 + i * kWarpsPerStepCta;
+            if (r >= P) break;
+            uint8_t* sb = wbuf + (size_t)i * a.sb_max;
+            const uint32_t e = __shfl_sync(FULL_MASK, my_e, i);
             if (s < 0) {
                 build_root(sb, L, lane);
-                warp_store(beam, sb, L.sbytes, lane);
-            } else {
-                warp_load(sb, beam + (int64_t)r * L.sbytes, L.sbytes, lane);
-            }
-            __syncwarp();
-            expand_gpu(sb, cb, L, d, st, a, r, s + 1, lane);
-            continue;
-        }
-        uint8_t* child = a.beam_pool + d.beam_off[(s + 1) & 1];
-        if (s < 0) {
-            build_root(sb, L, lane);
-            warp_store(child, sb, L.sbytes, lane);
-        } else {
-            const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
-            const uint32_t e = __ldg(a.sel + d.sel_off + r);
-            uint32_t* hrow = a.hist + d.hist_off + (int64_t)s * d.K;
-            if (mode == MODE_ICH || mode == MODE_PMS) {
-                const int c = (int)(e >> 8), i = (int)(e & 0xFFu);
-                warp_load(sb, parent + (int64_t)c * L.sbytes, L.sbytes, lane);
-                __syncwarp();
-                const int j = RD(sb, L)[i];
-                apply_child(sb, L, a.ops, d.op_off, i, true, ((uint32_t)c << 8) | (uint32_t)j,
-                            (uint32_t)(s + 1), lane);
-                warp_store(child + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
+                warp_store(childbuf, sb, L.sbytes, lane);
+            } else if (compat) {
+                const int c = (int)(e >> 8), ii = (int)(e & 0xFFu);
+                const int j = RD(sb, L)[ii];
+                apply_child<NQ>(sb, L, a.ops, d.op_off, ii, true, ((uint32_t)c << 8) | (uint32_t)j,
+                                (uint32_t)(s + 1), lane);
+                warp_store(childbuf + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
                 if (lane == 0) hrow[r] = ((uint32_t)c << 8) | (uint32_t)j;
-            } else {
+            } else if (mode != MODE_V1) {
                 const uint32_t slot = e & ~kFillerFlag;
                 const int c = (int)(slot / (uint32_t)L.n), b = (int)(slot % (uint32_t)L.n);
-                warp_load(sb, parent + (int64_t)c * L.sbytes, L.sbytes, lane);
-                __syncwarp();
-                ReadyOps R;
-                load_ready(sb, L, a.ops, d.op_off, lane, R);
-                Cands C;
-                pivot_candidates(R, d.seed + (uint32_t)s, (uint32_t)c, lane, C);
+                ReadyOps<NQ> R;
+                load_ready<NQ>(sb, L, a.ops, d.op_off, lane, R);
+                Cands<NQ> C;
+                pivot_candidates<NQ>(R, d.seed + (uint32_t)s, (uint32_t)c, lane, C);
                 if (b < C.cnt) {
                     // kernel_materialize_topk (gpu/v2_twophases/solver.cu:193-252)
-                    int i = -1, j = 0;
+                    int ii = -1, j = 0;
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        unsigned hit = __ballot_sync(FULL_MASK, ((C.bal[q] >> lane) & 1u) && C.bidx[q] == b);
+                    for (int qq = 0; qq < NQ; qq++) {
+                        unsigned hit = __ballot_sync(FULL_MASK, ((C.bal[qq] >> lane) & 1u) && C.bidx[qq] == b);
                         if (hit) {
                             const int l = __ffs(hit) - 1;
-                            i = 32 * q + l;
-                            j = __shfl_sync(FULL_MASK, R.job[q], l);
+                            ii = 32 * qq + l;
+                            j = __shfl_sync(FULL_MASK, R.job[qq], l);
                         }
                     }
-                    apply_child(sb, L, a.ops, d.op_off, i, false, ((uint32_t)c << 8) | (uint32_t)j,
-                                (uint32_t)(s + 1), lane);
-                    warp_store(child + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
+                    apply_child<NQ>(sb, L, a.ops, d.op_off, ii, false, ((uint32_t)c << 8) | (uint32_t)j,
+                                    (uint32_t)(s + 1), lane);
+                    warp_store(childbuf + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
                     if (lane == 0) hrow[r] = ((uint32_t)c << 8) | (uint32_t)j;
                 } else {
                     // filler rank: v2 leaves the ping-pong slot as it was (:191)
                     if (mode == MODE_CLEAN && lane == 0) atomicOr(&st.status, kStatusBadSelect);
                     __syncwarp();
-                    warp_load(sb, child + (int64_t)r * L.sbytes, L.sbytes, lane);
+                    warp_load(sb, childbuf + (int64_t)r * L.sbytes, L.sbytes, lane);
                     if (lane == 0) hrow[r] = kMark;
                 }
             }
+            __syncwarp();
+            if (compat) expand_compat<NQ>(sb, L, d, a, r, lane);
+            else {
+                const int rl = r - q * kChunk;
+                expand_gpu<NQ>(sb, cb, L, d, st, a, r, s + 1, lane, kstage + (size_t)rl * nst, &s_nv[rl], s_noise);
+            }
         }
-        __syncwarp();
-        if (mode == MODE_ICH || mode == MODE_PMS) expand_compat(sb, L, d, a, r, lane);
-        else expand_gpu(sb, cb, L, d, st, a, r, s + 1, lane);
+        __syncthreads();
+        if (!compat) {
+            // rank-ordered prefix of the staged counts, then coalesced copy-out
+            if (warp == 0) {
+                const int v = s_nv[lane];
+                int x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL_MASK, x, o);
+                    if (lane >= o) x += y;
+                }
+                s_pre[lane] = x - v;
+                if (lane == 31) s_kcnt = x;
+            }
+            __syncthreads();
+            for (int rl = warp; rl < kChunk; rl += kWarpsPerStepCta) {
+                const int cntk = s_nv[rl];
+                const int dst0 = s_pre[rl];
+                for (int i = lane; i < cntk; i += 32) kdst[dst0 + i] = kstage[(size_t)rl * nst + i];
+            }
+            if (threadIdx.x == 0) a.kcnt[d.kcnt_off + q] = s_kcnt;
+        }
+        __syncthreads();
     }
 }
 
@@ -420,27 +510,32 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a,
 // K-th key, survivors are compacted and bitonic-sorted in shared memory.
 // ------------------------------------------------------------------------------------
 struct SelSmem {
-    uint32_t* hist;           // [32][256]
-    uint32_t* tot;            // [256]
-    unsigned long long* red;  // [64]
-    int* misc;                // [64]
-    unsigned long long* sortbuf;
+    uint32_t* hist;            // 16 KB: u32[4096] bucket counts | u16[32][256] digit counters | u32[16][256]
+    uint32_t* tot;             // [256]
+    unsigned long long* red;   // [64]
+    int* misc;                 // [64]
+    unsigned long long* A;     // [kLsdMax]   compacted survivors / radix-sort buffer
+    unsigned long long* stg;   // [kStageKeys] staged candidate keys / radix-sort buffer / wide bitonic
 };
+
+constexpr int kLsdMax = 8192;      // largest survivor count for the radix sort
+constexpr int kStageKeys = 16384;  // candidate keys staged in shared memory
 
 __device__ __forceinline__ SelSmem sel_smem(uint8_t* base)
 {
     SelSmem s;
     s.hist = reinterpret_cast<uint32_t*>(base);
-    s.tot = s.hist + 32 * 256;
+    s.tot = s.hist + 4096;
     s.red = reinterpret_cast<unsigned long long*>(s.tot + 256);
     s.misc = reinterpret_cast<int*>(s.red + 64);
-    s.sortbuf = reinterpret_cast<unsigned long long*>(s.misc + 64);
+    s.A = reinterpret_cast<unsigned long long*>(s.misc + 64);
+    s.stg = s.A + kLsdMax;
     return s;
 }
 
-size_t select_smem_bytes(int sort_cap)
+size_t select_smem_bytes(int)
 {
-    return (size_t)(32 * 256 + 256) * 4 + 64 * 8 + 64 * 4 + (size_t)sort_cap * 8;
+    return (size_t)(4096 + 256) * 4 + 64 * 8 + 64 * 4 + (size_t)(kLsdMax + kStageKeys) * 8;
 }
 
 // Block-wide exclusive scan of one int per thread; returns the prefix, *total the sum.
@@ -474,39 +569,140 @@ __device__ int block_exclusive_scan(int v, int* total, int* warp_sums)
     return res;
 }
 
-template <bool REG>
-__device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int s, uint8_t* smem)
-{
-    constexpr int KPT = 16;
-    SelSmem S = sel_smem(smem);
-    int* wsum = reinterpret_cast<int*>(S.hist);  // scan scratch (hist is free outside passes)
-    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
-    const int P = st.P, V = st.V, n = d.n, K = d.K;
-    const int total = P * n;
-    int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
-    const int R = V < keff ? V : keff;
-    const unsigned long long* keys = a.keys + d.key_off;
-
-    unsigned long long kr[REG ? KPT : 1];
-    if (REG) {
+// Candidate keys of one beam live in per-chunk regions of cap keys each, filled to
+// cpref[c+1]-cpref[c]; logical key i is found by a binary search over the prefix.
+struct KeySrc {
+    const unsigned long long* base;
+    const int* cpref;  // shared memory, nch+1 entries
+    int nch;
+    int cap;
+    __device__ __forceinline__ unsigned long long operator()(int i) const
+    {
+        int lo = 0, hi = nch;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (cpref[mid] <= i) lo = mid; else hi = mid;
+        }
+        return base[(size_t)lo * cap + (i - cpref[lo])];
+    }
+    // keys i0 .. i0+KPT-1 (~0 past V): one search, then walk the chunks
+    template <int KPT>
+    __device__ __forceinline__ void load_run(int i0, int V, unsigned long long (&out)[KPT]) const
+    {
+        int lo = 0, hi = nch;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (cpref[mid] <= i0) lo = mid; else hi = mid;
+        }
 #pragma unroll
-        for (int q = 0; q < (REG ? KPT : 1); q++) {
-            int idx = tid + q * nthr;
-            kr[q] = idx < V ? keys[idx] : ~0ull;
+        for (int q = 0; q < KPT; q++) {
+            const int i = i0 + q;
+            if (i < V) {
+                while (lo + 1 < nch && cpref[lo + 1] <= i) lo++;
+                out[q] = base[(size_t)lo * cap + (i - cpref[lo])];
+            } else {
+                out[q] = ~0ull;
+            }
         }
     }
+};
 
+// ---- top-K selection -----------------------------------------------------------------
+// 1. stage: the level's candidate keys (slot order) into shared memory, coalesced.
+// 2. threshold: one histogram pass over 4096 linear buckets of the score bits gives the
+//    bucket T holding rank R; every key of buckets <= T is kept (R plus the rest of T).
+//    If that set is too large, MSD radix passes over the 64-bit keys find the R-th key
+//    exactly instead.
+// 3. compact the kept keys, stably (slot order preserved), with one block scan.
+// 4. stable LSD radix sort by the score bits only -- the input is in slot order, so this
+//    is exactly the reference's stable (score, slot) order -- and emit the first R.
+constexpr int kNB = 4096;
+
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a < b ? b : a; }
+
+__device__ __forceinline__ int pow2ceil(int c)
+{
+    return c <= 1 ? 1 : 1 << (32 - __clz(c - 1));
+}
+
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem_src) : "memory");
+}
+
+// 1. all V keys, logical order, into stg (warp per chunk, consecutive lanes -> consecutive keys)
+__device__ void stage_keys(const KeySrc& ks, unsigned long long* stg)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int c = warp; c < ks.nch; c += nwarps) {
+        const int c0 = ks.cpref[c], nc = ks.cpref[c + 1] - c0;
+        const unsigned long long* src = ks.base + (size_t)c * ks.cap;
+        for (int i = lane; i < nc; i += 32) cp_async8(stg + c0 + i, src + i);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+}
+
+// 2a. bucket threshold: returns the number of keys in buckets <= T; misc[2] = T,
+// misc[4] = shift, misc[1] = smin.
+template <typename Get>
+__device__ int bucket_threshold(Get get, int V, int R, const SelSmem& S)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
+    uint32_t* cnt = S.hist;
+    int* misc = S.misc;
+    int* wsum = reinterpret_cast<int*>(S.red);
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+    for (int i = tid; i < V; i += nthr) { uint32_t sb = (uint32_t)(get(i) >> 32); mn = min(mn, sb); mx = max(mx, sb); }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+        mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    }
+    for (int b = tid; b < kNB; b += nthr) cnt[b] = 0;
+    if (tid == 0) { misc[0] = 0; misc[1] = (int)0xFFFFFFFFu; }
+    __syncthreads();
+    if (lane == 0) {
+        atomicMax(reinterpret_cast<unsigned*>(&misc[0]), mx);
+        atomicMin(reinterpret_cast<unsigned*>(&misc[1]), mn);
+    }
+    __syncthreads();
+    const uint32_t smin = (uint32_t)misc[1], range = (uint32_t)misc[0] - smin;
+    const int nbits = range ? 32 - __clz(range) : 0;
+    const int shift = nbits > 12 ? nbits - 12 : 0;
+    for (int i = tid; i < V; i += nthr) atomicAdd(&cnt[(((uint32_t)(get(i) >> 32)) - smin) >> shift], 1u);
+    __syncthreads();
+    constexpr int BPT = kNB / kSelectThreads;
+    uint32_t c4[BPT];
+    int sum = 0;
+#pragma unroll
+    for (int u = 0; u < BPT; u++) { c4[u] = cnt[tid * BPT + u]; sum += (int)c4[u]; }
+    int tot;
+    int base = block_exclusive_scan(sum, &tot, wsum);
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        if (base < R && R <= base + (int)c4[u]) { misc[2] = tid * BPT + u; misc[3] = base + (int)c4[u]; }
+        base += (int)c4[u];
+    }
+    if (tid == 0) misc[4] = shift;
+    __syncthreads();
+    return misc[3];
+}
+
+// 2b. radix threshold: exact R-th key; returns (pmask, prefix) with keep = (k & pmask) <= prefix.
+template <typename Get>
+__device__ void radix_threshold(Get get, int V, int R, const SelSmem& S, unsigned long long& pmask_out,
+                                unsigned long long& prefix_out)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
     unsigned long long pmask = 0ull, prefix = 0ull;
     if (V > R && R > 0) {
         // --- min / max -> highest differing bit ---
         unsigned long long mn = ~0ull, mx = 0ull;
-        if (REG) {
-#pragma unroll
-            for (int q = 0; q < (REG ? KPT : 1); q++)
-                if (tid + q * nthr < V) { mn = min(mn, kr[q]); mx = max(mx, kr[q]); }
-        } else {
-            for (int idx = tid; idx < V; idx += nthr) { unsigned long long k = keys[idx]; mn = min(mn, k); mx = max(mx, k); }
-        }
+        for (int idx = tid; idx < V; idx += nthr) { unsigned long long k = get(idx); mn = min(mn, k); mx = max(mx, k); }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
@@ -533,25 +729,17 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
             const int db = shift < 8 ? shift : 8;
             shift -= db;
             const unsigned dm = (1u << db) - 1u;
-            for (int t = tid; t < 32 * 256; t += nthr) S.hist[t] = 0;
+            for (int t = tid; t < 16 * 256; t += nthr) S.hist[t] = 0;
             __syncthreads();
-            uint32_t* hw = S.hist + warp * 256;
-            if (REG) {
-#pragma unroll
-                for (int q = 0; q < (REG ? KPT : 1); q++) {
-                    unsigned long long k = kr[q];
-                    if (tid + q * nthr < V && (k & pmask) == prefix) atomicAdd(hw + ((unsigned)(k >> shift) & dm), 1u);
-                }
-            } else {
-                for (int idx = tid; idx < V; idx += nthr) {
-                    unsigned long long k = keys[idx];
-                    if ((k & pmask) == prefix) atomicAdd(hw + ((unsigned)(k >> shift) & dm), 1u);
-                }
+            uint32_t* hw = S.hist + (warp & 15) * 256;
+            for (int idx = tid; idx < V; idx += nthr) {
+                unsigned long long k = get(idx);
+                if ((k & pmask) == prefix) atomicAdd(hw + ((unsigned)(k >> shift) & dm), 1u);
             }
             __syncthreads();
             for (int t = tid; t < 256; t += nthr) {
                 uint32_t sum = 0;
-                for (int w = 0; w < (nthr >> 5); w++) sum += S.hist[w * 256 + t];
+                for (int w = 0; w < 16; w++) sum += S.hist[w * 256 + t];
                 S.tot[t] = sum;
             }
             __syncthreads();
@@ -592,120 +780,384 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
         }
     }
 
-    // --- compact survivors ((key & pmask) <= prefix) into sortbuf ---
-    int nsurv = 0;
-    if (R > 0) {
-        if (REG) {
-            int cnt = 0;
-#pragma unroll
-            for (int q = 0; q < (REG ? KPT : 1); q++)
-                if (tid + q * nthr < V && (kr[q] & pmask) <= prefix) cnt++;
-            int tot;
-            int off = block_exclusive_scan(cnt, &tot, wsum);
-#pragma unroll
-            for (int q = 0; q < (REG ? KPT : 1); q++)
-                if (tid + q * nthr < V && (kr[q] & pmask) <= prefix && off < R) S.sortbuf[off++] = kr[q];
-            nsurv = tot;
-        } else {
-            int base = 0;
-            for (int i0 = 0; i0 < V; i0 += nthr) {
-                int idx = i0 + tid;
-                unsigned long long k = idx < V ? keys[idx] : ~0ull;
-                int f = (idx < V && (k & pmask) <= prefix) ? 1 : 0;
-                int tot;
-                int off = block_exclusive_scan(f, &tot, wsum);
-                if (f && base + off < R) S.sortbuf[base + off] = k;
-                base += tot;
-            }
-            nsurv = base;
-        }
-    }
-    if (nsurv != R) {
-        if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
-        nsurv = nsurv < R ? nsurv : R;
-    }
+    pmask_out = pmask;
+    prefix_out = prefix;
+    __syncthreads();
+}
 
-    // --- bitonic sort of the survivors ---
-    if (R > 1) {
-        int ns = 1;
-        while (ns < R) ns <<= 1;
-        for (int t = R + tid; t < ns; t += nthr) S.sortbuf[t] = ~0ull;
+// 3. stable compaction: each warp owns a contiguous range of the input, counted then
+// written tile by tile with ballots; one block scan over the 32 warp totals.
+template <typename Get, typename Keep>
+__device__ int compact_stable(Get get, int V, Keep keep, unsigned long long* dst, int cap, const SelSmem& S)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    int* wtot = S.misc + 16;   // [32]
+    const int L = ((V + nwarps - 1) / nwarps + 31) & ~31;
+    const int lo = warp * L, hi = min(V, lo + L);
+    int c = 0;
+    for (int i0 = lo; i0 < hi; i0 += 32) {
+        const int i = i0 + lane;
+        c += __popc(__ballot_sync(FULL_MASK, i < hi && keep(get(i))));
+    }
+    if (lane == 0) wtot[warp] = c;
+    __syncthreads();
+    if (warp == 0) {
+        const int v = lane < nwarps ? wtot[lane] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < nwarps) wtot[lane] = x - v;
+        if (lane == 31) S.misc[60] = x;
+    }
+    __syncthreads();
+    int pos = wtot[warp];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int i0 = lo; i0 < hi; i0 += 32) {
+        const int i = i0 + lane;
+        unsigned long long k = 0;
+        bool f = false;
+        if (i < hi) { k = get(i); f = keep(k); }
+        const unsigned b = __ballot_sync(FULL_MASK, f);
+        if (f && pos + __popc(b & lt) < cap) dst[pos + __popc(b & lt)] = k;
+        pos += __popc(b);
+    }
+    const int total = S.misc[60];
+    __syncthreads();
+    return total;
+}
+
+// 4. stable LSD radix sort of `count` (<= kLsdMax) keys by their score bits, first R out.
+// Elements p = warp*32*E + e*32 + lane are ranked in element order against per-warp
+// 16-bit digit counters with bit-ballot peer masks (no atomics); a digit-major prefix over
+// (digit, warp) gives the scatter base.
+template <int E>
+__device__ void lsd_sort_emit(unsigned long long* A, unsigned long long* B, int count, int R, uint32_t* sel,
+                              const SelSmem& S)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    uint16_t* wh = reinterpret_cast<uint16_t*>(S.hist);   // [32][256]
+    int* dtot = reinterpret_cast<int*>(S.tot);
+    int* misc = S.misc;
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int p = warp * 32 * E + e * 32 + lane;
+        if (p < count) { const uint32_t sb = (uint32_t)(A[p] >> 32); mn = min(mn, sb); mx = max(mx, sb); }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+        mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    }
+    if (tid == 0) { misc[8] = 0; misc[9] = (int)0xFFFFFFFFu; }
+    __syncthreads();
+    if (lane == 0) {
+        atomicMax(reinterpret_cast<unsigned*>(&misc[8]), mx);
+        atomicMin(reinterpret_cast<unsigned*>(&misc[9]), mn);
+    }
+    __syncthreads();
+    const uint32_t smin = (uint32_t)misc[9];
+    const uint32_t range = (uint32_t)misc[8] - smin;
+    const int nbits = (count > 0 && range) ? 32 - __clz(range) : 0;
+    for (int sh = 0; sh < nbits; sh += 8) {
+        uint32_t* wh32 = S.hist;
+        for (int i = tid; i < 32 * 256 / 2; i += blockDim.x) wh32[i] = 0;
         __syncthreads();
-        for (int k = 2; k <= ns; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int pi = tid; pi < (ns >> 1); pi += nthr) {
-                    const int lo = ((pi & ~(j - 1)) << 1) | (pi & (j - 1));
-                    const int hi = lo + j;
-                    const bool up = (lo & k) == 0;
-                    unsigned long long x = S.sortbuf[lo], y = S.sortbuf[hi];
-                    if ((x > y) == up) { S.sortbuf[lo] = y; S.sortbuf[hi] = x; }
-                }
-                const int nj = (j > 1) ? (j >> 1) : (k << 1) >> 1;
-                if (j >= 64 || nj >= 64) __syncthreads(); else __syncwarp();
+        unsigned long long x[E];
+        int dg[E], off[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int p = warp * 32 * E + e * 32 + lane;
+            const bool valid = p < count;
+            x[e] = valid ? A[p] : 0ull;
+            const int d = valid ? (int)(((((uint32_t)(x[e] >> 32)) - smin) >> sh) & 255u) : 0;
+            // lanes holding the same digit: intersect the 8 bit-ballots
+            unsigned grp = __ballot_sync(FULL_MASK, valid);
+#pragma unroll
+            for (int bit = 0; bit < 8; bit++) {
+                const unsigned bb = __ballot_sync(FULL_MASK, (d >> bit) & 1);
+                grp &= ((d >> bit) & 1) ? bb : ~bb;
             }
+            const int r_in = __popc(grp & lt);
+            int b = 0;
+            if (valid) b = wh[warp * 256 + d];
+            __syncwarp();
+            if (valid && r_in == 0) wh[warp * 256 + d] = (uint16_t)(b + __popc(grp));
+            __syncwarp();
+            dg[e] = d;
+            off[e] = b + r_in;
         }
         __syncthreads();
-    } else {
+        // per digit: exclusive prefix over the 32 warps (thread d walks the warps; the
+        // [warp][256] layout makes consecutive threads read consecutive counters)
+        if (tid < 256) {
+            int run = 0;
+            for (int w = 0; w < 32; w++) {
+                const int t = wh[w * 256 + tid];
+                wh[w * 256 + tid] = (uint16_t)run;
+                run += t;
+            }
+            dtot[tid] = run;
+        }
         __syncthreads();
+        if (warp == 0) {
+            int v8[8], sum = 0;
+#pragma unroll
+            for (int u = 0; u < 8; u++) { v8[u] = dtot[lane * 8 + u]; sum += v8[u]; }
+            int xx = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, xx, o);
+                if (lane >= o) xx += y;
+            }
+            int run = xx - sum;
+#pragma unroll
+            for (int u = 0; u < 8; u++) { dtot[lane * 8 + u] = run; run += v8[u]; }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int p = warp * 32 * E + e * 32 + lane;
+            if (p < count) B[dtot[dg[e]] + (int)wh[warp * 256 + dg[e]] + off[e]] = x[e];
+        }
+        __syncthreads();
+        unsigned long long* t = A;
+        A = B;
+        B = t;
     }
+    for (int i = tid; i < R; i += blockDim.x) sel[i] = (uint32_t)(A[i] & 0xFFFFFFFFull);
+}
+
+// in-thread compare-exchange stage of distance J (< E) on the blocked layout i = t*E + e
+template <int E, int J>
+__device__ __forceinline__ void bitonic_in_thread(unsigned long long (&x)[E], int t, int k)
+{
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        if ((e & J) == 0) {
+            const bool up = ((t * E + e) & k) == 0;
+            const unsigned long long a = x[e], b = x[e + J];
+            if ((a > b) == up) { x[e] = b; x[e + J] = a; }
+        }
+    }
+}
+
+// Ascending bitonic sort of N = 1024*E keys, E per thread (thread t holds positions
+// t*E .. t*E+E-1); xs is a shared exchange buffer of N keys, used striped (e*1024 + t) so
+// cross-warp stages are bank-conflict free.
+template <int E>
+__device__ void block_bitonic_reg(unsigned long long (&x)[E], unsigned long long* xs)
+{
+    const int t = threadIdx.x, lane = t & 31;
+    const int N = E * kSelectThreads;
+    for (int k = 2; k <= N; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j < E) {
+                if (j == 1) bitonic_in_thread<E, 1>(x, t, k);
+                else if (j == 2) bitonic_in_thread<E, (E > 2 ? 2 : 1)>(x, t, k);
+                else if (j == 4) bitonic_in_thread<E, (E > 4 ? 4 : 1)>(x, t, k);
+                else bitonic_in_thread<E, (E > 8 ? 8 : 1)>(x, t, k);
+            } else if (j < 32 * E) {
+                const int lj = j / E;
+                const bool low = (lane & lj) == 0;
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const bool up = ((t * E + e) & k) == 0;
+                    const unsigned long long y = __shfl_xor_sync(FULL_MASK, x[e], lj);
+                    x[e] = (low == up) ? umin64(x[e], y) : umax64(x[e], y);
+                }
+            } else {
+                const int tj = j / E;
+#pragma unroll
+                for (int e = 0; e < E; e++) xs[e * kSelectThreads + t] = x[e];
+                __syncthreads();
+                const bool low = (t & tj) == 0;
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const bool up = ((t * E + e) & k) == 0;
+                    const unsigned long long y = xs[e * kSelectThreads + (t ^ tj)];
+                    x[e] = (low == up) ? umin64(x[e], y) : umax64(x[e], y);
+                }
+                __syncthreads();
+            }
+        }
+    }
+}
+
+template <int E>
+__device__ void sort_emit_e(unsigned long long* sbuf, int count, int R, uint32_t* sel)
+{
+    const int t = threadIdx.x;
+    unsigned long long x[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int idx = e * kSelectThreads + t;   // any bijection works for unsorted input
+        x[e] = idx < count ? sbuf[idx] : ~0ull;
+    }
+    __syncthreads();
+    block_bitonic_reg<E>(x, sbuf);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int i = t * E + e;
+        if (i < R) sel[i] = (uint32_t)(x[e] & 0xFFFFFFFFull);
+    }
+}
+
+// Sort the `count` keys in sbuf and write the first R slots to sel (count <= 16384).
+__device__ void sort_and_emit(unsigned long long* sbuf, int count, int R, uint32_t* sel)
+{
+    const int N = pow2ceil(count);
+    if (N <= kSelectThreads) sort_emit_e<1>(sbuf, count, R, sel);
+    else if (N <= 2 * kSelectThreads) sort_emit_e<2>(sbuf, count, R, sel);
+    else if (N <= 4 * kSelectThreads) sort_emit_e<4>(sbuf, count, R, sel);
+    else if (N <= 8 * kSelectThreads) sort_emit_e<8>(sbuf, count, R, sel);
+    else sort_emit_e<16>(sbuf, count, R, sel);
+}
+
+// Fillers (v1 / v2 only): when fewer than min(P*n, K) children were scored, the
+// reference's stable sort keeps the lowest-numbered unscored slots next, in slot order.
+__device__ void select_fillers(const SegDesc& d, const StepArgs& a, int P, int R, int keff, uint32_t* sel,
+                               uint8_t* smem)
+{
+    if (keff <= R) return;
+    int* wsum = reinterpret_cast<int*>(smem);
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int n = d.n;
+    const int F = keff - R;
+    const int W = d.words;
+    const uint32_t* mk = a.masks + d.mask_off;
+    int base = 0;
+    for (int c0 = 0; c0 < P && base < F; c0 += nthr) {
+        const int c = c0 + tid;
+        int f = 0;
+        if (c < P) {
+            int pc = 0;
+            for (int w = 0; w < W; w++) pc += __popc(mk[(int64_t)c * W + w]);
+            f = n - pc;
+        }
+        int tot;
+        const int off = block_exclusive_scan(f, &tot, wsum);
+        if (c < P && base + off < F) {
+            int out = R + base + off;
+            const int lim = F - base - off;
+            int got = 0;
+            for (int b = 0; b < n && got < lim && got < f; b++) {
+                uint32_t word = mk[(int64_t)c * W + (b >> 5)];
+                if (!((word >> (b & 31)) & 1u)) {
+                    sel[out + got] = kFillerFlag | (uint32_t)(c * n + b);
+                    got++;
+                }
+            }
+        }
+        base += tot;
+    }
+}
+
+__device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int V, const KeySrc& ks,
+                           uint8_t* smem)
+{
+    const int tid = threadIdx.x;
+    const int P = st.P, K = d.K;
+    const int total = P * d.n;
+    const int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
+    const int R = V < keff ? V : keff;
     uint32_t* sel = a.sel + d.sel_off;
-    for (int r = tid; r < R; r += nthr) sel[r] = (uint32_t)(S.sortbuf[r] & 0xFFFFFFFFull);
-
-    // --- fillers: the lowest-numbered unscored slots (v1 / v2 only) ---
-    if (keff > R) {
-        const int F = keff - R;
-        const int W = d.words;
-        const uint32_t* mk = a.masks + d.mask_off;
-        int base = 0;
-        for (int c0 = 0; c0 < P && base < F; c0 += nthr) {
-            const int c = c0 + tid;
-            int f = 0;
-            if (c < P) {
-                int pc = 0;
-                for (int w = 0; w < W; w++) pc += __popc(mk[(int64_t)c * W + w]);
-                f = n - pc;
+    const SelSmem S = sel_smem(smem);
+    if (R > 0) {
+        // staged (shared-memory) input when the level fits, else read from global memory
+        const bool staged = (V <= kStageKeys) && (K <= kLsdMax);
+        if (staged) stage_keys(ks, S.stg);
+        const unsigned long long* stg = S.stg;
+        auto get_s = [=](int i) { return stg[i]; };
+        auto get_g = [=](int i) { return ks(i); };
+        int count = staged ? bucket_threshold(get_s, V, R, S) : bucket_threshold(get_g, V, R, S);
+        unsigned long long* dst = S.A;
+        const int T = S.misc[2], shift = S.misc[4];
+        const uint32_t smin = (uint32_t)S.misc[1];
+        __syncthreads();
+        if (count <= kLsdMax) {
+            const uint32_t lim = ((uint32_t)T + 1u) << shift;  // bucket <= T
+            auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
+            count = staged ? compact_stable(get_s, V, keep, dst, kLsdMax, S)
+                           : compact_stable(get_g, V, keep, dst, kLsdMax, S);
+        } else {
+            if (tid == 0) st.select_fallbacks += 1;
+            unsigned long long pmask, prefix;
+            if (staged) radix_threshold(get_s, V, R, S, pmask, prefix);
+            else radix_threshold(get_g, V, R, S, pmask, prefix);
+            auto keep = [=](unsigned long long k) { return (k & pmask) <= prefix; };
+            if (R > kLsdMax) dst = S.stg;  // only reached unstaged (K > kLsdMax)
+            const int cap = (R > kLsdMax) ? kStageKeys : kLsdMax;
+            count = staged ? compact_stable(get_s, V, keep, dst, cap, S)
+                           : compact_stable(get_g, V, keep, dst, cap, S);
+        }
+        if (count < R || count > kStageKeys) {
+            if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
+            count = count > kStageKeys ? kStageKeys : count;
+        }
+        const int RR = R < count ? R : count;
+        if (count <= kLsdMax) {
+            const int E = (count + kSelectThreads - 1) / kSelectThreads;
+            unsigned long long* B = S.stg;
+            switch (E) {
+            case 0:
+            case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
+            case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
+            case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
+            case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
+            case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
+            case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
+            case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
+            default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
             }
-            int tot;
-            const int off = block_exclusive_scan(f, &tot, wsum);
-            if (c < P && base + off < F) {
-                int out = R + base + off;
-                const int lim = F - base - off;
-                int got = 0;
-                for (int b = 0; b < n && got < lim && got < f; b++) {
-                    uint32_t word = mk[(int64_t)c * W + (b >> 5)];
-                    if (!((word >> (b & 31)) & 1u)) {
-                        sel[out + got] = kFillerFlag | (uint32_t)(c * n + b);
-                        got++;
-                    }
-                }
-            }
-            base += tot;
+        } else {
+            sort_and_emit(S.stg, count, RR, sel);
         }
     }
     __syncthreads();
+    select_fillers(d, a, P, R, keff, sel, smem);
+    __syncthreads();
     if (tid == 0) {
         st.P = keff;
-        st.V = 0;
         st.materialized += keff;
     }
 }
 
-__global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s)
+__global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, int sort_cap)
 {
     extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_cpref[kMaxChunks + 1];
+    __shared__ int s_wsum[72];
+    (void)sort_cap;
     const int seg = blockIdx.x;
     const SegDesc& d = a.segs[seg];
     if (d.mode > MODE_CLEAN || s >= d.N) return;
     SegState& st = a.st[seg];
+    // candidate counts of the level's chunks -> prefix, V
+    const int nch = (d.K + kChunk - 1) / kChunk;
+    const int c = threadIdx.x;
+    const int v = (c < nch) ? a.kcnt[d.kcnt_off + c] : 0;
+    int V;
+    const int pre = block_exclusive_scan(v, &V, s_wsum);
+    if (c < nch) s_cpref[c] = pre;
+    if (c == 0) s_cpref[nch] = V;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        st.expanded += st.V;
+        st.expanded += V;
         st.slots += (long long)st.P * d.n;
         if (st.P > 0) st.levels += 1;
     }
     if (s == d.N - 1) return;  // the last level's sort and gather are not observable
-    __syncthreads();
-    if (st.V <= 16 * kSelectThreads) select_gpu<true>(d, st, a, s, smem);
-    else select_gpu<false>(d, st, a, s, smem);
+    KeySrc ks;
+    ks.base = a.keys + d.key_off;
+    ks.cpref = s_cpref;
+    ks.nch = nch;
+    ks.cap = kChunk * d.n;
+    select_gpu(d, st, a, V, ks, smem);
 }
 
 // ------------------------------------------------------------------------------------
@@ -984,9 +1436,14 @@ __global__ void k_finalize(StepArgs a)
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
-size_t step_smem_bytes(int sb_max) { return (size_t)kWarpsPerStepCta * 2 * sb_max; }
+size_t step_smem_bytes(int sb_max, int max_n)
+{
+    return (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * sb_max + (size_t)kChunk * max_n * 8;
+}
 
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max)
+int nq_class(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
+
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n)
 {
     cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem_bytes(sort_cap));
@@ -994,8 +1451,11 @@ cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_m
     e = cudaFuncSetAttribute(k_heap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)heap_smem_bytes(max_k, stage_bytes));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)step_smem_bytes(sb_max));
+    e = cudaFuncSetAttribute(k_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
 }
 
 template <typename F>
@@ -1008,16 +1468,23 @@ static cudaError_t raise_smem(F* fn, size_t bytes)
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t raise_kernel_smem(int sort_cap, int sb_max)
+cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
 {
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
     if (e != cudaSuccess) return e;
-    return raise_smem(k_step, step_smem_bytes(sb_max));
+    e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
+    if (e != cudaSuccess) return e;
+    e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
+    if (e != cudaSuccess) return e;
+    return raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
 }
 
-cudaError_t launch_step(const StepArgs& a, int s, int grid, cudaStream_t stream)
+cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
-    k_step<<<grid, kWarpsPerStepCta * 32, step_smem_bytes(a.sb_max), stream>>>(a, s);
+    const size_t sm = step_smem_bytes(a.sb_max, a.max_n);
+    if (nq_mask & 2) k_step<1><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
+    if (nq_mask & 4) k_step<2><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
+    if (nq_mask & 16) k_step<4><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
     return cudaGetLastError();
 }
 
@@ -1029,7 +1496,7 @@ cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t st
 
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream)
 {
-    k_select<<<a.nseg, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s);
+    k_select<<<a.nseg, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s, sort_cap);
     return cudaGetLastError();
 }
 

@@ -13,9 +13,13 @@ struct StepArgs {
     const SegDesc* segs;
     SegState* st;
     const int32_t* rank_prefix;   // [nseg+1] prefix sums of K (flattened rank space)
+    const int32_t* chunk_prefix;  // [nseg+1] prefix sums of ceil(K/kChunk)
+    int32_t* kcnt;                // candidate keys per chunk of the current level
     int32_t nseg;
     int32_t total_ranks;
+    int32_t total_chunks;
     int32_t sb_max;               // per-warp state buffer bytes (max sbytes)
+    int32_t max_n;                // largest n of the batch (k_step key staging)
     int32_t pad0;
     uint8_t* beam_pool;
     uint8_t* slot_pool;
@@ -30,20 +34,23 @@ struct StepArgs {
 };
 
 // Grid / shared-memory sizing helpers.
-size_t step_smem_bytes(int sb_max);
+size_t step_smem_bytes(int sb_max, int max_n);
 size_t select_smem_bytes(int sort_cap);
 size_t heap_smem_bytes(int max_k, int stage_bytes);
 
 // Launchers (asynchronous on `stream`).
-cudaError_t launch_step(const StepArgs& a, int s, int grid, cudaStream_t stream);
+// k_step is instantiated per NQ = ceil(n/32) in {1, 2, 4}; nq_mask has bit NQ set for
+// each class present in the batch (one launch per class).
+cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream);
+int nq_class(int n);
 cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream);
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream);
 cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
                         cudaStream_t stream);
 cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream);
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max);
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n);
 // Raise (never lower) the dynamic shared-memory limits of k_select and k_step to what
 // a launch with `sort_cap` / `sb_max` needs.
-cudaError_t raise_kernel_smem(int sort_cap, int sb_max);
+cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n);
 
 }  // namespace bsj

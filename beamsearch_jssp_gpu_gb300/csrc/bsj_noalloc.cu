@@ -121,16 +121,21 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     d.auxbytes = 16;
     d.group = 0;
     d.op_off = 0;
+    d.nq = nq_class(n);
+    d.kcnt_off = 0;
+    const int nch = (beam_width + kChunk - 1) / kChunk;
     const size_t K = (size_t)beam_width, N = (size_t)d.N;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return at; };
     const size_t o_seg = take(sizeof(SegDesc));
     const size_t o_state = take(sizeof(SegState));
     const size_t o_prefix = take(2 * sizeof(int32_t));
+    const size_t o_cprefix = take(2 * sizeof(int32_t));
+    const size_t o_kcnt = take((size_t)nch * sizeof(int32_t));
     const size_t o_group = take(sizeof(int32_t));
     const size_t o_ops = take(N * sizeof(uint32_t));
     const size_t o_beam = take(2 * align_up(K * d.sbytes, 256));
-    const size_t o_keys = take(K * n * 8);
+    const size_t o_keys = take((size_t)nch * kChunk * n * 8);
     const size_t o_sel = take(K * 4);
     const size_t o_mask = take(K * d.words * 4);
     const size_t o_hist = take(N * K * 4);
@@ -151,6 +156,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     st.best = ~0ull;
     st.best_cmax = kSentinel;
     const int32_t prefix[2] = {0, beam_width};
+    const int32_t cprefix[2] = {0, nch};
     const int32_t group = best_known;
 
     StepArgs a{};
@@ -159,7 +165,11 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     a.rank_prefix = reinterpret_cast<const int32_t*>(base + o_prefix);
     a.nseg = 1;
     a.total_ranks = beam_width;
+    a.chunk_prefix = reinterpret_cast<const int32_t*>(base + o_cprefix);
+    a.total_chunks = nch;
+    a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
     a.sb_max = d.sbytes;
+    a.max_n = n;
     a.beam_pool = base + o_beam;
     a.slot_pool = nullptr;
     a.keys = reinterpret_cast<unsigned long long*>(base + o_keys);
@@ -176,23 +186,25 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     int sms = 0, dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return BSJ_ERR_CUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return BSJ_ERR_CUDA;
-    if (raise_kernel_smem(sort_cap, d.sbytes) != cudaSuccess) return BSJ_ERR_CUDA;
-    const int grid = std::max(1, std::min((beam_width + kWarpsPerStepCta - 1) / kWarpsPerStepCta, sms * 8));
+    if (raise_kernel_smem(sort_cap, d.sbytes, n) != cudaSuccess) return BSJ_ERR_CUDA;
+    const int grid = std::max(1, std::min(nch, sms * 4));
+    const int nq_mask = 1 << d.nq;
 
     // everything that must start at zero or at its initial value is rewritten here
     cudaError_t e = cudaMemcpyAsync(base + o_seg, &d, sizeof(d), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_state, &st, sizeof(st), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_prefix, prefix, sizeof(prefix), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_cprefix, cprefix, sizeof(cprefix), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_group, &group, sizeof(group), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(base + o_beam, 0, 2 * align_up(K * d.sbytes, 256), s);
     if (e != cudaSuccess) return BSJ_ERR_CUDA;
     k_noalloc_pack<<<1, 256, 0, s>>>(d_machine, d_duration, d.N, m, reinterpret_cast<uint32_t*>(base + o_ops),
                                      reinterpret_cast<SegState*>(base + o_state));
     if (cudaGetLastError() != cudaSuccess) return BSJ_ERR_CUDA;
-    if (launch_step(a, -1, grid, s) != cudaSuccess) return BSJ_ERR_CUDA;
+    if (launch_step(a, -1, grid, nq_mask, s) != cudaSuccess) return BSJ_ERR_CUDA;
     for (int lv = 0; lv < d.N; lv++) {
         if (launch_select(a, lv, sort_cap, s) != cudaSuccess) return BSJ_ERR_CUDA;
-        if (lv < d.N - 1 && launch_step(a, lv, grid, s) != cudaSuccess) return BSJ_ERR_CUDA;
+        if (lv < d.N - 1 && launch_step(a, lv, grid, nq_mask, s) != cudaSuccess) return BSJ_ERR_CUDA;
     }
     if (launch_finalize(a, s) != cudaSuccess) return BSJ_ERR_CUDA;
     k_noalloc_out<<<1, 256, 0, s>>>(reinterpret_cast<const SegState*>(base + o_state),

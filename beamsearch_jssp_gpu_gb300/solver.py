@@ -182,9 +182,11 @@ class Plan:
         selb = ctypes.c_double()
         e = ctypes.c_int64()
         mat = ctypes.c_int64()
+        fb = ctypes.c_int64()
         self.ctx._check(self.lib.bsj_plan_stats(self.h, ctypes.byref(sb), ctypes.byref(selb), ctypes.byref(e),
-                                                ctypes.byref(mat)))
-        return dict(step_bytes=sb.value, select_bytes=selb.value, expanded=e.value, materialized=mat.value)
+                                                ctypes.byref(mat), ctypes.byref(fb)))
+        return dict(step_bytes=sb.value, select_bytes=selb.value, expanded=e.value, materialized=mat.value,
+                    select_fallbacks=fb.value)
 
     def set_timing(self, on: bool):
         self.ctx._check(self.lib.bsj_plan_set_timing(self.h, 1 if on else 0))

@@ -289,6 +289,7 @@ def gpu_arm(args) -> int:
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk,
+                "select_fallback_levels": stats["select_fallbacks"],
                 "makespans": [r["makespan"] for r in res]}
         print(json.dumps(line), flush=True)
     plan.close()

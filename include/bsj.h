@@ -128,9 +128,10 @@ int64_t bsj_plan_launches(const bsj_plan *plan);
 /* Algorithmic bytes of the last run, per kernel class: k_step -- per materialised
    survivor one parent snapshot read, one child snapshot written, its 4 B survivor id and
    4 B history entry, plus 8 B per emitted candidate key; k_select -- 8 B per candidate
-   key read, 4 B per survivor id written.  Also the run's expanded children and survivors. */
+   key read, 4 B per survivor id written.  Also the run's expanded children, survivors and
+   the number of levels whose top-K fell back from the bucket path to the radix path. */
 bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, double *select_bytes,
-                          int64_t *expanded, int64_t *materialized);
+                          int64_t *expanded, int64_t *materialized, int64_t *select_fallbacks);
 /* When enabled, bsj_plan_run records CUDA events around every launch of each kernel
    class; bsj_plan_kernel_ms returns total ms per class and launch counts for the last run:
    index 0 k_step, 1 k_select, 2 k_heap, 3 k_gather_v1, 4 k_finalize. */
