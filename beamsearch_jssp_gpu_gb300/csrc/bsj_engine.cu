@@ -25,15 +25,21 @@
 
 using namespace bsj;
 
+constexpr int kMaxBranches = 8;
+
 struct bsj_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t branch[kMaxBranches] = {};  // independent beam groups run on these
     std::string err;
     int sm_count = 0;
     int max_smem_optin = 0;
     // grow-only device arena reused by bsj_solve / bsj_solve_batch
     void* arena = nullptr;
     size_t arena_bytes = 0;
+    // plans of recent batch shapes (most recent last), reused with new data
+    std::vector<std::pair<std::string, bsj_plan*>> cache;
+    uint64_t hits = 0;
 };
 
 struct bsj_plan {
@@ -47,6 +53,16 @@ struct bsj_plan {
     int sort_cap = 0, heap_k = 0, heap_chunk = 1, heap_stage = 16;
     bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
     int step_grid = 1;
+    // beam groups: contiguous beam ranges run as independent graph branches, so one
+    // group's select overlaps the others' expansion
+    struct Group {
+        StepArgs args;
+        int maxN = 0, nq_mask = 0, step_grid = 1, gather_grid = 1;
+        bool has_v1 = false, has_gpu = false, has_compat = false;
+    };
+    std::vector<Group> groups;
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kMaxBranches] = {};
     std::vector<SegDesc> segs;
     std::vector<SegState> init;
     std::vector<int32_t> prefix;
@@ -335,6 +351,12 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.rank_prefix = p->d_prefix;
     a.nseg = nbeams;
     a.total_ranks = p->total_ranks;
+    a.seg_lo = 0;
+    a.seg_hi = nbeams;
+    a.chunk_lo = 0;
+    a.chunk_hi = p->total_chunks;
+    a.rank_lo = 0;
+    a.rank_hi = p->total_ranks;
     a.chunk_prefix = p->d_cprefix;
     a.total_chunks = p->total_chunks;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
@@ -374,10 +396,52 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return cuda_fail(ctx, e, "configure kernels");
     }
     // warps of k_step: one per rank, 8 per CTA, up to 8 CTAs per SM resident
-    // k_step: one CTA per chunk of kChunk ranks, at most 4 resident per SM
-    p->step_grid = std::max(1, std::min(p->total_chunks, ctx->sm_count * 4));
+    // k_step: one CTA per chunk of kChunk ranks
+    p->step_grid = std::max(1, std::min(p->total_chunks, 65535));
     int want = (p->total_ranks + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
     p->gather_grid = std::max(1, std::min(want, ctx->sm_count * 8));
+    // beam groups, balanced by work (K * levels)
+    {
+        const int G = std::min(nbeams, kMaxBranches);
+        double total = 0;
+        for (int b = 0; b < nbeams; b++) total += (double)p->segs[b].K * p->segs[b].N;
+        int lo = 0;
+        double acc = 0;
+        for (int g = 0; g < G && lo < nbeams; g++) {
+            int hi = lo + 1;
+            acc += (double)p->segs[lo].K * p->segs[lo].N;
+            const double target = total * (g + 1) / G;
+            while (hi < nbeams && (nbeams - hi) > (G - 1 - g) && acc + 0.5 * (double)p->segs[hi].K * p->segs[hi].N <= target) {
+                acc += (double)p->segs[hi].K * p->segs[hi].N;
+                hi++;
+            }
+            if (g == G - 1) {
+                while (hi < nbeams) { acc += (double)p->segs[hi].K * p->segs[hi].N; hi++; }
+            }
+            bsj_plan::Group gr;
+            gr.args = p->args;
+            gr.args.seg_lo = lo;
+            gr.args.seg_hi = hi;
+            gr.args.chunk_lo = p->cprefix[lo];
+            gr.args.chunk_hi = p->cprefix[hi];
+            gr.args.rank_lo = p->prefix[lo];
+            gr.args.rank_hi = p->prefix[hi];
+            for (int b = lo; b < hi; b++) {
+                const SegDesc& d = p->segs[b];
+                gr.maxN = std::max(gr.maxN, d.N);
+                gr.nq_mask |= 1 << d.nq;
+                if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
+                if (d.mode <= BSJ_MODE_CLEAN) gr.has_gpu = true; else gr.has_compat = true;
+            }
+            gr.step_grid = std::max(1, std::min(p->cprefix[hi] - p->cprefix[lo], 65535));
+            const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
+            gr.gather_grid = std::max(1, std::min(wr, ctx->sm_count * 8));
+            p->groups.push_back(gr);
+            lo = hi;
+        }
+        cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+        for (int g = 0; g < (int)p->groups.size(); g++) cudaEventCreateWithFlags(&p->join[g], cudaEventDisableTiming);
+    }
     *out = p;
     return BSJ_OK;
 }
@@ -427,27 +491,113 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
         if (p->slot_bytes) e = cudaMemsetAsync(a.slot_pool, 0, p->slot_bytes, s);
         if (e != cudaSuccess) return e;
     }
-    e = timed(0, [&] { return launch_step(a, -1, p->step_grid, p->nq_mask, s); });
-    if (e != cudaSuccess) return e;
-    for (int lv = 0; lv < p->maxN; lv++) {
-        if (p->has_gpu) {
-            e = timed(1, [&] { return launch_select(a, lv, p->sort_cap, s); });
-            if (e != cudaSuccess) return e;
-        }
-        if (p->has_compat) {
-            e = timed(2, [&] { return launch_heap(a, lv, p->heap_k, p->heap_chunk, p->heap_stage, s); });
-            if (e != cudaSuccess) return e;
-        }
-        if (lv < p->maxN - 1) {
-            if (p->has_v1) {
-                e = timed(3, [&] { return launch_gather_v1(a, lv, p->gather_grid, s); });
-                if (e != cudaSuccess) return e;
+    // one beam group's level loop on stream gs
+    auto group_loop = [&](const bsj_plan::Group& gr, cudaStream_t gs) -> cudaError_t {
+        auto rec = [&](cudaEvent_t ev) {
+            return capturing ? cudaEventRecordWithFlags(ev, gs, cudaEventRecordExternal) : cudaEventRecord(ev, gs);
+        };
+        auto timed_g = [&](int cls, auto&& fn) -> cudaError_t {
+            if (!p->timing) { p->launches++; return fn(); }
+            cudaEvent_t* ev = next_events(p, cls);
+            cudaError_t r = rec(ev[0]);
+            if (r != cudaSuccess) return r;
+            r = fn();
+            if (r != cudaSuccess) return r;
+            p->launches++;
+            return rec(ev[1]);
+        };
+        const StepArgs& ga = gr.args;
+        cudaError_t r = timed_g(0, [&] { return launch_step(ga, -1, gr.step_grid, gr.nq_mask, gs); });
+        if (r != cudaSuccess) return r;
+        for (int lv = 0; lv < gr.maxN; lv++) {
+            if (gr.has_gpu) {
+                r = timed_g(1, [&] { return launch_select(ga, lv, p->sort_cap, gs); });
+                if (r != cudaSuccess) return r;
             }
-            e = timed(0, [&] { return launch_step(a, lv, p->step_grid, p->nq_mask, s); });
+            if (gr.has_compat) {
+                r = timed_g(2, [&] { return launch_heap(ga, lv, p->heap_k, p->heap_chunk, p->heap_stage, gs); });
+                if (r != cudaSuccess) return r;
+            }
+            if (lv < gr.maxN - 1) {
+                if (gr.has_v1) {
+                    r = timed_g(3, [&] { return launch_gather_v1(ga, lv, gr.gather_grid, gs); });
+                    if (r != cudaSuccess) return r;
+                }
+                r = timed_g(0, [&] { return launch_step(ga, lv, gr.step_grid, gr.nq_mask, gs); });
+                if (r != cudaSuccess) return r;
+            }
+        }
+        return cudaSuccess;
+    };
+    if (p->groups.size() <= 1) {
+        e = group_loop(p->groups[0], s);
+        if (e != cudaSuccess) return e;
+    } else {
+        e = cudaEventRecord(p->fork, s);
+        if (e != cudaSuccess) return e;
+        for (size_t g = 0; g < p->groups.size(); g++) {
+            cudaStream_t gs = p->ctx->branch[g];
+            e = cudaStreamWaitEvent(gs, p->fork, 0);
+            if (e != cudaSuccess) return e;
+            e = group_loop(p->groups[g], gs);
+            if (e != cudaSuccess) return e;
+            e = cudaEventRecord(p->join[g], gs);
+            if (e != cudaSuccess) return e;
+            e = cudaStreamWaitEvent(s, p->join[g], 0);
             if (e != cudaSuccess) return e;
         }
     }
     return timed(4, [&] { return launch_finalize(a, s); });
+}
+
+constexpr size_t kPlanCache = 4;
+
+// Everything that fixes a plan's layout and graph: sizes, modes, widths, bound groups.
+std::string shape_key(int ninst, const bsj_instance* insts, int nbeams, const bsj_beam* beams)
+{
+    std::string k = std::to_string(ninst) + "|";
+    for (int i = 0; i < ninst; i++) k += std::to_string(insts[i].n) + "x" + std::to_string(insts[i].m) + ",";
+    k += "|";
+    for (int b = 0; b < nbeams; b++)
+        k += std::to_string(beams[b].mode) + ":" + std::to_string(beams[b].beam_width) + ":" +
+             std::to_string(beams[b].instance) + ":" + std::to_string(beams[b].bound_group) + ",";
+    return k;
+}
+
+// New instance data, seeds and bounds into a plan of the same shape.
+bsj_status plan_refresh(bsj_plan* p, int ninst, const bsj_instance* insts, const bsj_beam* beams)
+{
+    bsj_context* ctx = p->ctx;
+    for (int i = 0; i < ninst; i++) {
+        bsj_status s = validate_instance(ctx, insts[i]);
+        if (s != BSJ_OK) return s;
+    }
+    std::vector<uint32_t> ops;
+    for (int i = 0; i < ninst; i++)
+        for (int64_t q = 0; q < (int64_t)insts[i].n * insts[i].m; q++)
+            ops.push_back(((uint32_t)insts[i].duration[q] << 8) | (uint32_t)insts[i].machine[q]);
+    std::fill(p->group_init.begin(), p->group_init.end(), INT32_MAX);
+    for (int b = 0; b < p->nseg; b++) {
+        const bsj_beam& bm = beams[b];
+        p->segs[b].seed = bm.seed;
+        SegState st{};
+        st.P = 1;
+        st.bound = bm.best_known;
+        st.best = ~0ull;
+        st.best_cmax = kSentinel;
+        if (bm.mode > BSJ_MODE_CLEAN) glibc_rand_state(bm.seed, st.rng, &st.rng_i);
+        p->init[b] = st;
+        const int g = p->seg_group[b];
+        p->group_init[g] = std::min(p->group_init[g], bm.best_known);
+    }
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(p->d_segs, p->segs.data(), sizeof(SegDesc) * p->nseg, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * p->nseg, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(const_cast<uint32_t*>(p->args.ops), ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "plan refresh");
+    return BSJ_OK;
 }
 
 }  // namespace
@@ -486,6 +636,8 @@ bsj_status bsj_create(bsj_context** out, int device)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (int g = 0; g < kMaxBranches && e == cudaSuccess; g++)
+        e = cudaStreamCreateWithFlags(&ctx->branch[g], cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete ctx; return BSJ_ERR_CUDA; }
     ctx->device = device;
     *out = ctx;
@@ -496,8 +648,12 @@ void bsj_destroy(bsj_context* ctx)
 {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    for (auto& kv : ctx->cache) bsj_plan_destroy(kv.second);
+    ctx->cache.clear();
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    for (cudaStream_t b : ctx->branch)
+        if (b) cudaStreamDestroy(b);
     delete ctx;
 }
 
@@ -574,6 +730,9 @@ void bsj_plan_destroy(bsj_plan* p)
     cudaSetDevice(p->ctx->device);
     for (cudaGraphExec_t g : p->graph)
         if (g) cudaGraphExecDestroy(g);
+    if (p->fork) cudaEventDestroy(p->fork);
+    for (cudaEvent_t ev : p->join)
+        if (ev) cudaEventDestroy(ev);
     for (auto& ev : p->events) {
         cudaEventDestroy(ev.second.first);
         cudaEventDestroy(ev.second.second);
@@ -585,9 +744,14 @@ void bsj_plan_destroy(bsj_plan* p)
 int64_t bsj_plan_launches(const bsj_plan* p)
 {
     if (!p) return 0;
-    // fixed by the plan shape: 1 + maxN*(select? + heap?) + (maxN-1)*(gather_v1? + step) + 1
-    int64_t per = (p->has_gpu ? 1 : 0) + (p->has_compat ? 1 : 0);
-    int64_t n = 2 + (int64_t)p->maxN * per + (int64_t)(p->maxN - 1) * (1 + (p->has_v1 ? 1 : 0));
+    // fixed by the plan shape: per group 1 + maxN*(select? + heap?) + (maxN-1)*(gather_v1? + step
+    // launches per NQ class); one finalize
+    int64_t n = 1;
+    for (const auto& gr : p->groups) {
+        const int64_t per = (gr.has_gpu ? 1 : 0) + (gr.has_compat ? 1 : 0);
+        const int64_t nq = __builtin_popcount((unsigned)gr.nq_mask);
+        n += nq + (int64_t)gr.maxN * per + (int64_t)(gr.maxN - 1) * (nq + (gr.has_v1 ? 1 : 0));
+    }
     return n;
 }
 
@@ -646,19 +810,38 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan* p, float* ms, int64_t* launches, i
 bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instance* instances,
                            int num_beams, const bsj_beam* beams, bsj_result* results, void* stream)
 {
-    if (!ctx || !results) return BSJ_ERR_INVALID;
+    if (!ctx || !results || !instances || !beams || num_instances < 1 || num_beams < 1) return BSJ_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    bsj_plan* p = nullptr;
-    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, true, &p);
-    if (s != BSJ_OK) return s;
-    // eager launches: a one-shot plan gains nothing from graph capture
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const std::string key = shape_key(num_instances, instances, num_beams, beams);
+    for (size_t i = 0; i < ctx->cache.size(); i++) {
+        if (ctx->cache[i].first != key) continue;
+        // same shape as a recent call: new data into the existing plan, replay its graph
+        bsj_plan* p = ctx->cache[i].second;
+        std::rotate(ctx->cache.begin() + i, ctx->cache.begin() + i + 1, ctx->cache.end());
+        bsj_status s = plan_refresh(p, num_instances, instances, beams);
+        if (s != BSJ_OK) return s;
+        ctx->hits++;
+        p->timing = false;
+        s = bsj_plan_run(p, st);
+        if (s != BSJ_OK) return s;
+        return bsj_plan_results(p, results);
+    }
+    bsj_plan* p = nullptr;
+    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, false, &p);
+    if (s != BSJ_OK) return s;
+    // first call of this shape: eager launches (capturing a graph pays off on reuse only)
     p->last_stream = st;
     cudaError_t e = enqueue_run(p, st, false);
     if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
     s = bsj_plan_results(p, results);
-    bsj_plan_destroy(p);
-    return s;
+    if (s != BSJ_OK) { bsj_plan_destroy(p); return s; }
+    if (ctx->cache.size() >= kPlanCache) {
+        bsj_plan_destroy(ctx->cache.front().second);
+        ctx->cache.erase(ctx->cache.begin());
+    }
+    ctx->cache.push_back({key, p});
+    return BSJ_OK;
 }
 
 bsj_status bsj_solve(bsj_context* ctx, const bsj_instance* inst, const bsj_beam* beam,

@@ -181,20 +181,21 @@ __device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int o
         }
         __syncwarp();
     }
-    if (lane == 0) {
-        TR(b)[mc] = fin;
-        JR(b, L)[j] = fin;
-        if (!erase) RD(b, L)[i] = RD(b, L)[r - 1];
-        int rr = r - 1;
-        if (k + 1 < L.m) RD(b, L)[rr++] = (uint8_t)j;
-        NX(b, L)[j] = (uint8_t)(k + 1);
-        *H_R(b, L) = (uint16_t)rr;
-        *H_NS(b, L) = (uint16_t)(*H_NS(b, L) + 1);
-        int cm = *H_CMAX(b, L);
-        *H_CMAX(b, L) = cm > fin ? cm : fin;
-        *H_LIN(b, L) = lineage;
-        *H_STAMP(b, L) = stamp;
-    }
+    // the edits touch distinct bytes: one lane each
+    const uint8_t last = RD(b, L)[r - 1];
+    const int ns = *H_NS(b, L), cm = *H_CMAX(b, L);
+    const bool cont = (k + 1 < L.m);
+    __syncwarp();
+    if (lane == 0) TR(b)[mc] = fin;
+    if (lane == 1) JR(b, L)[j] = fin;
+    if (lane == 2 && !erase && i != r - 1) RD(b, L)[i] = last;
+    if (lane == 3 && cont) RD(b, L)[r - 1] = (uint8_t)j;
+    if (lane == 4) NX(b, L)[j] = (uint8_t)(k + 1);
+    if (lane == 5)
+        *reinterpret_cast<uint32_t*>(b + L.off_hdr) = ((uint32_t)(ns + 1) << 16) | (uint32_t)(r - 1 + (cont ? 1 : 0));
+    if (lane == 6) *H_CMAX(b, L) = cm > fin ? cm : fin;
+    if (lane == 7) *H_LIN(b, L) = lineage;
+    if (lane == 8) *H_STAMP(b, L) = stamp;
     __syncwarp();
 }
 
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int 
         smem + (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * a.sb_max);
     for (int k = threadIdx.x; k < 1000; k += blockDim.x)
         s_noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
-    for (int chunk = blockIdx.x; chunk < a.total_chunks; chunk += gridDim.x) {
+    for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
         const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
         const SegDesc& d = a.segs[seg];
         if (d.nq != NQ || s >= d.N - 1) continue;
@@ -478,7 +479,7 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a,
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = gridDim.x * kWarpsPerStepCta;
-    for (int flat = blockIdx.x * kWarpsPerStepCta + warp; flat < a.total_ranks; flat += nw) {
+    for (int flat = a.rank_lo + blockIdx.x * kWarpsPerStepCta + warp; flat < a.rank_hi; flat += nw) {
         const int seg = find_seg(a.rank_prefix, a.nseg, flat);
         const SegDesc& d = a.segs[seg];
         if (d.mode != MODE_V1 || s >= d.N - 1) continue;
@@ -834,8 +835,7 @@ __device__ int compact_stable(Get get, int V, Keep keep, unsigned long long* dst
 // 16-bit digit counters with bit-ballot peer masks (no atomics); a digit-major prefix over
 // (digit, warp) gives the scatter base.
 template <int E>
-__device__ void lsd_sort_emit(unsigned long long* A, unsigned long long* B, int count, int R, uint32_t* sel,
-                              const SelSmem& S)
+__device__ unsigned long long* lsd_sort(unsigned long long* A, unsigned long long* B, int count, const SelSmem& S)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -929,7 +929,33 @@ __device__ void lsd_sort_emit(unsigned long long* A, unsigned long long* B, int 
         A = B;
         B = t;
     }
-    for (int i = tid; i < R; i += blockDim.x) sel[i] = (uint32_t)(A[i] & 0xFFFFFFFFull);
+    return A;
+}
+
+template <int E>
+__device__ void lsd_sort_emit(unsigned long long* A, unsigned long long* B, int count, int R, uint32_t* sel,
+                              const SelSmem& S)
+{
+    const unsigned long long* out = lsd_sort<E>(A, B, count, S);
+    for (int i = threadIdx.x; i < R; i += blockDim.x) sel[i] = (uint32_t)(out[i] & 0xFFFFFFFFull);
+}
+
+// Any element count up to 8 per thread.
+__device__ unsigned long long* lsd_sort_any(unsigned long long* A, unsigned long long* B, int count,
+                                            const SelSmem& S)
+{
+    const int E = (count + (int)blockDim.x - 1) / (int)blockDim.x;
+    switch (E) {
+    case 0:
+    case 1: return lsd_sort<1>(A, B, count, S);
+    case 2: return lsd_sort<2>(A, B, count, S);
+    case 3: return lsd_sort<3>(A, B, count, S);
+    case 4: return lsd_sort<4>(A, B, count, S);
+    case 5: return lsd_sort<5>(A, B, count, S);
+    case 6: return lsd_sort<6>(A, B, count, S);
+    case 7: return lsd_sort<7>(A, B, count, S);
+    default: return lsd_sort<8>(A, B, count, S);
+    }
 }
 
 // in-thread compare-exchange stage of distance J (< E) on the blocked layout i = t*E + e
@@ -1133,7 +1159,7 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     __shared__ int s_cpref[kMaxChunks + 1];
     __shared__ int s_wsum[72];
     (void)sort_cap;
-    const int seg = blockIdx.x;
+    const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
     if (d.mode > MODE_CLEAN || s >= d.N) return;
     SegState& st = a.st[seg];
@@ -1250,7 +1276,7 @@ struct Rng {
 __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    const int seg = blockIdx.x;
+    const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
     if (d.mode < MODE_ICH || s >= d.N) return;
     SegState& st = a.st[seg];
@@ -1443,10 +1469,28 @@ size_t step_smem_bytes(int sb_max, int max_n)
 
 int nq_class(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
 
+// All level kernels run back to back; giving them one shared-memory carveout (the
+// maximum) keeps the SMs from being reconfigured between k_select and k_step.
+static cudaError_t set_carveout()
+{
+    const int c = cudaSharedmemCarveoutMaxShared;
+    cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<1>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<2>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<4>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gather_v1, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    return e;
+}
+
 cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n)
 {
+    cudaError_t ec = set_carveout();
+    if (ec != cudaSuccess) return ec;
     cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)select_smem_bytes(sort_cap));
+
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_heap, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)heap_smem_bytes(max_k, stage_bytes));
@@ -1496,14 +1540,14 @@ cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t st
 
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream)
 {
-    k_select<<<a.nseg, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s, sort_cap);
+    k_select<<<a.seg_hi - a.seg_lo, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s, sort_cap);
     return cudaGetLastError();
 }
 
 cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
                         cudaStream_t stream)
 {
-    k_heap<<<a.nseg, kHeapThreads, heap_smem_bytes(max_k, stage_bytes), stream>>>(a, s, chunk, stage_bytes);
+    k_heap<<<a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes), stream>>>(a, s, chunk, stage_bytes);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,11 @@ struct StepArgs {
     int32_t total_chunks;
     int32_t sb_max;               // per-warp state buffer bytes (max sbytes)
     int32_t max_n;                // largest n of the batch (k_step key staging)
+    // the beams this launch works on: [seg_lo, seg_hi) and their chunk / rank ranges
+    // (several ranges run as independent branches of one graph)
+    int32_t seg_lo, seg_hi;
+    int32_t chunk_lo, chunk_hi;
+    int32_t rank_lo, rank_hi;
     int32_t pad0;
     uint8_t* beam_pool;
     uint8_t* slot_pool;

@@ -165,6 +165,12 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     a.rank_prefix = reinterpret_cast<const int32_t*>(base + o_prefix);
     a.nseg = 1;
     a.total_ranks = beam_width;
+    a.seg_lo = 0;
+    a.seg_hi = 1;
+    a.chunk_lo = 0;
+    a.chunk_hi = nch;
+    a.rank_lo = 0;
+    a.rank_hi = beam_width;
     a.chunk_prefix = reinterpret_cast<const int32_t*>(base + o_cprefix);
     a.total_chunks = nch;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
@@ -187,7 +193,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     if (cudaGetDevice(&dev) != cudaSuccess) return BSJ_ERR_CUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return BSJ_ERR_CUDA;
     if (raise_kernel_smem(sort_cap, d.sbytes, n) != cudaSuccess) return BSJ_ERR_CUDA;
-    const int grid = std::max(1, std::min(nch, sms * 4));
+    const int grid = std::max(1, nch);
     const int nq_mask = 1 << d.nq;
 
     // everything that must start at zero or at its initial value is rewritten here

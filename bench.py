@@ -203,37 +203,44 @@ def gpu_arm(args) -> int:
     ctx = Context(local)
     beams = [BeamSpec(MODE, K, 500000, BEAMS * rank + b, 0, 0) for b in range(BEAMS)]
     plan = ctx.plan([(mc, du)], beams)
-    plan.set_timing(True)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()            # explicit stream: a handle of 0 would select the context's own
     sh = stream.cuda_stream
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
-    for _ in range(args.warmup):
-        plan.run(sh)
-    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        plan.set_timing(False)
+        for _ in range(args.warmup):
+            plan.run(sh)
+        torch.cuda.synchronize()
 
-    clocks = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    times = []
-    for _ in range(args.steps):
+        clocks = ClockSampler(local)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        times = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(sh)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        clk = clocks.stop()
+        stats = plan.stats()
+        res = plan.results(with_sequence=False)
+        # per-kernel device times: one more step of the same plan with CUDA events around
+        # every launch (event nodes slow the graph, so they stay out of the timed steps)
+        plan.set_timing(True)
         flush.fill_(1)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
         plan.run(sh)
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    kms = plan.kernel_ms()           # per-kernel device time of the last timed step
-    stats = plan.stats()
-    res = plan.results(with_sequence=False)
+        torch.cuda.synchronize()
+        kms = plan.kernel_ms()
     expanded = sum(r["expanded"] for r in res)
     launches_per_step = plan.launches
     t_step = sum(times) / len(times)
@@ -250,15 +257,16 @@ def gpu_arm(args) -> int:
 
     # e2e: the C ABI from host buffers (instance upload + all levels + results/schedules back)
     e2e_times = []
-    for k in range(args.warmup + args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        out = ctx.solve_batch([(mc, du)], beams, sh)
-        t1 = time.perf_counter()
-        if k >= args.warmup:
-            e2e_times.append(t1 - t0)
-        assert sum(r["expanded"] for r in out) == expanded
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = ctx.solve_batch([(mc, du)], beams, sh)
+            t1 = time.perf_counter()
+            if k >= args.warmup:
+                e2e_times.append(t1 - t0)
+            assert sum(r["expanded"] for r in out) == expanded
     e2e_t = sum(e2e_times) / len(e2e_times)
     if dist:
         tt = torch.tensor([e2e_t], device="cuda")
@@ -267,7 +275,7 @@ def gpu_arm(args) -> int:
     h2d = mc.nbytes + du.nbytes + 24 * BEAMS
     d2h = BEAMS * (N_JOBS * N_MACH * 4 + 48)
 
-    # roofline of the dominant kernel (live CUDA-event times of the last timed step)
+    # roofline of the dominant kernel (CUDA-event times of the profiled step)
     peaks = _peaks()
     alg = {"k_step": stats["step_bytes"], "k_select": stats["select_bytes"]}
     dom = max(("k_step", "k_select"), key=lambda k: kms[k][0])
