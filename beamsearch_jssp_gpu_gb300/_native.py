@@ -13,6 +13,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libbsj.so")
 
 BSJ_OK = 0
+BSJ_ERR_INVALID = 1
+BSJ_ERR_LIMIT = 2
+BSJ_ERR_CUDA = 3
+BSJ_ERR_NOMEM = 4
+BSJ_ERR_DEVICE = 5
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "size outside the supported limits",
                 3: "CUDA error", 4: "out of memory", 5: "device-side consistency check failed"}
 MODES = {"v1": 0, "v2": 1, "clean": 2, "ich": 3, "pms": 4}
@@ -25,6 +30,7 @@ EXPORTED = [
     "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations", "bsj_plan_create", "bsj_plan_run",
     "bsj_plan_results", "bsj_plan_destroy", "bsj_plan_launches", "bsj_plan_stats",
     "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_solve_noalloc",
+    "bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count",
 ]
 
 
@@ -84,7 +90,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_solve_batch.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam), P(Result), vp]
     L.bsj_solve_iterations.argtypes = [vp, P(Instance), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, P(ctypes.c_uint32), ctypes.c_int32,
-                                       P(ctypes.c_int32), P(ctypes.c_int32), vp]
+                                       P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32), vp]
     L.bsj_plan_create.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam), P(vp)]
     L.bsj_plan_run.argtypes = [vp, vp]
     L.bsj_plan_results.argtypes = [vp, P(Result)]
@@ -100,6 +106,15 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_solve_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int32, ctypes.c_uint32, vp, vp]
     L.bsj_solve_noalloc.restype = ctypes.c_int
+    # host-side instance files and schedule decoding (no device needed)
+    L.bsj_instance_resolve.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]
+    L.bsj_instance_read.argtypes = [ctypes.c_char_p, P(ctypes.c_int32), P(ctypes.c_int32),
+                                    P(ctypes.c_int32), P(ctypes.c_int32), ctypes.c_int32]
+    L.bsj_schedule_decode.argtypes = [P(Instance), P(ctypes.c_int32), P(ctypes.c_int32),
+                                      P(ctypes.c_int32)]
+    L.bsj_device_count.argtypes = [P(ctypes.c_int32)]
+    for name in ("bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count"):
+        getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
                  "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
                  "bsj_plan_set_timing", "bsj_plan_kernel_ms"):

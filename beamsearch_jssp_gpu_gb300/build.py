@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libbsj.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
-SOURCES = ["bsj_kernels.cu", "bsj_engine.cu", "bsj_compat.cpp", "bsj_noalloc.cu"]
+SOURCES = ["bsj_kernels.cu", "bsj_engine.cu", "bsj_compat.cpp", "bsj_noalloc.cu", "bsj_instance.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr"]
@@ -80,7 +80,38 @@ def build(verbose: bool = False, force: bool = False) -> str:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link of libbsj.so failed")
         os.replace(tmp, LIB)
+    build_cli(force=force)
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "bsj_cli.cpp")
+CLI_BIN = os.path.join(OUT_DIR, "bsj_cli")
+# names the reference's Makefile gives its drivers (Makefile:55-95); each is a link to bsj_cli
+CLI_NAMES = ["exec_gpu_v1", "exec_gpu_v2", "exec_gpu_v1_bench", "exec_gpu_v2_bench", "BS-ICH", "BS-PMS",
+             "BS-PMS-bench", "exec_time_width"]
+
+
+def build_cli(force: bool = False) -> str:
+    """Compile the command-line drivers against libbsj.so (host C++ only) and link the
+    reference's driver names to them in _lib/."""
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    if force or _stale(CLI_BIN, [CLI_SRC, LIB] + [os.path.join(inc, h) for h in os.listdir(inc)]):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        tmp = CLI_BIN + ".tmp"
+        cmd = [cxx, "-O2", "-std=c++17", "-Wall", CLI_SRC, "-o", tmp, "-L" + OUT_DIR, "-lbsj",
+               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("build of bsj_cli failed")
+        os.replace(tmp, CLI_BIN)
+    for name in CLI_NAMES:
+        link = os.path.join(OUT_DIR, name)
+        if not os.path.islink(link):
+            if os.path.exists(link):
+                os.remove(link)
+            os.symlink("bsj_cli", link)
+    return CLI_BIN
 
 
 if __name__ == "__main__":

@@ -82,7 +82,7 @@ struct SegState {
     int32_t levels;
     int32_t makespan;
     int32_t found;
-    uint32_t rng_i;
+    uint32_t rng_i;       // ICH/PMS rand() stream: position of the next value, in [34, 68)
     uint32_t rng[34];
 };
 

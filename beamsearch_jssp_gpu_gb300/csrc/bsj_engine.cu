@@ -120,6 +120,7 @@ bsj_status cuda_fail(bsj_context* ctx, cudaError_t e, const char* what)
 // glibc srand()/rand() state (published algorithm of glibc random_r.c, TYPE_3): r[0] =
 // seed (1 if 0), r[i] = 16807*r[i-1] mod (2^31-1) for i < 31 via Schrage's method,
 // r[i] = r[i-31] for 31..33, r[i] = r[i-31] + r[i-3] afterwards; outputs start at r[344].
+// ring[i mod 34] holds r[i] for the last 34 positions.
 void glibc_rand_state(uint32_t seed, uint32_t ring[34], uint32_t* next_index)
 {
     std::vector<uint32_t> r(344);
@@ -134,7 +135,7 @@ void glibc_rand_state(uint32_t seed, uint32_t ring[34], uint32_t* next_index)
     for (int k = 31; k < 34; k++) r[k] = r[k - 31];
     for (int k = 34; k < 344; k++) r[k] = r[k - 31] + r[k - 3];
     for (int k = 310; k < 344; k++) ring[k % 34] = r[k];
-    *next_index = 344;
+    *next_index = 34 + 344 % 34;  // position 344, kept in [34, 68) like the device stream
 }
 
 bsj_status validate_instance(bsj_context* ctx, const bsj_instance& in)
@@ -600,6 +601,46 @@ bsj_status plan_refresh(bsj_plan* p, int ninst, const bsj_instance* insts, const
     return BSJ_OK;
 }
 
+// The rand() stream of an ICH/PMS beam, carried from one pass to the next the way the
+// process-wide state runs on between the reference's successive calls
+// (cpu/v1_pms/main.cpp:56,64).
+struct RandCarry {
+    uint32_t i;  // position of the next value, in [34, 68)
+    uint32_t r[34];
+};
+
+// Start each ICH/PMS beam of the plan's next run from `in[b]` instead of its seed.
+bsj_status plan_put_rand(bsj_plan* p, const RandCarry* in)
+{
+    for (int b = 0; b < p->nseg; b++) {
+        if (p->segs[b].mode <= BSJ_MODE_CLEAN) continue;
+        p->init[b].rng_i = 34 + (in[b].i % 34);
+        std::memcpy(p->init[b].rng, in[b].r, sizeof(in[b].r));
+    }
+    cudaStream_t st = p->ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * p->nseg,
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? BSJ_OK : cuda_fail(p->ctx, e, "rand state upload");
+}
+
+// Where each ICH/PMS beam's stream stands after the last run (call after the results).
+bsj_status plan_get_rand(bsj_plan* p, RandCarry* out)
+{
+    std::vector<SegState> st(p->nseg);
+    cudaError_t e = cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p->ctx, e, "rand state read");
+    for (int b = 0; b < p->nseg; b++) {
+        out[b].i = st[b].rng_i;
+        std::memcpy(out[b].r, st[b].rng, sizeof(out[b].r));
+    }
+    return BSJ_OK;
+}
+
+bsj_status solve_batch_impl(bsj_context* ctx, int num_instances, const bsj_instance* instances,
+                            int num_beams, const bsj_beam* beams, bsj_result* results, void* stream,
+                            const RandCarry* rand_in, RandCarry* rand_out);
+
 }  // namespace
 
 // =====================================================================================
@@ -608,6 +649,16 @@ bsj_status plan_refresh(bsj_plan* p, int ninst, const bsj_instance* insts, const
 extern "C" {
 
 const char* bsj_version(void) { return kVersion; }
+
+bsj_status bsj_device_count(int32_t* count)
+{
+    if (!count) return BSJ_ERR_INVALID;
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    *count = (e == cudaSuccess) ? c : 0;
+    if (e != cudaSuccess) cudaGetLastError();
+    return e == cudaSuccess ? BSJ_OK : BSJ_ERR_CUDA;
+}
 
 const char* bsj_status_string(bsj_status s)
 {
@@ -810,6 +861,17 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan* p, float* ms, int64_t* launches, i
 bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instance* instances,
                            int num_beams, const bsj_beam* beams, bsj_result* results, void* stream)
 {
+    return solve_batch_impl(ctx, num_instances, instances, num_beams, beams, results, stream, nullptr, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+
+bsj_status solve_batch_impl(bsj_context* ctx, int num_instances, const bsj_instance* instances,
+                            int num_beams, const bsj_beam* beams, bsj_result* results, void* stream,
+                            const RandCarry* rand_in, RandCarry* rand_out)
+{
     if (!ctx || !results || !instances || !beams || num_instances < 1 || num_beams < 1) return BSJ_ERR_INVALID;
     cudaSetDevice(ctx->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
@@ -820,21 +882,28 @@ bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instan
         bsj_plan* p = ctx->cache[i].second;
         std::rotate(ctx->cache.begin() + i, ctx->cache.begin() + i + 1, ctx->cache.end());
         bsj_status s = plan_refresh(p, num_instances, instances, beams);
+        if (s == BSJ_OK && rand_in) s = plan_put_rand(p, rand_in);
         if (s != BSJ_OK) return s;
         ctx->hits++;
         p->timing = false;
         s = bsj_plan_run(p, st);
-        if (s != BSJ_OK) return s;
-        return bsj_plan_results(p, results);
+        if (s == BSJ_OK) s = bsj_plan_results(p, results);
+        if (s == BSJ_OK && rand_out) s = plan_get_rand(p, rand_out);
+        return s;
     }
     bsj_plan* p = nullptr;
     bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, false, &p);
+    if (s == BSJ_OK && rand_in) {
+        s = plan_put_rand(p, rand_in);
+        if (s != BSJ_OK) bsj_plan_destroy(p);
+    }
     if (s != BSJ_OK) return s;
     // first call of this shape: eager launches (capturing a graph pays off on reuse only)
     p->last_stream = st;
     cudaError_t e = enqueue_run(p, st, false);
     if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
     s = bsj_plan_results(p, results);
+    if (s == BSJ_OK && rand_out) s = plan_get_rand(p, rand_out);
     if (s != BSJ_OK) { bsj_plan_destroy(p); return s; }
     if (ctx->cache.size() >= kPlanCache) {
         bsj_plan_destroy(ctx->cache.front().second);
@@ -843,6 +912,10 @@ bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instan
     ctx->cache.push_back({key, p});
     return BSJ_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 bsj_status bsj_solve(bsj_context* ctx, const bsj_instance* inst, const bsj_beam* beam,
                      bsj_result* result, void* stream)
@@ -855,9 +928,15 @@ bsj_status bsj_solve(bsj_context* ctx, const bsj_instance* inst, const bsj_beam*
 
 bsj_status bsj_solve_iterations(bsj_context* ctx, const bsj_instance* inst, int mode, int beam_width,
                                 int num_beams, int iterations, const uint32_t* seeds,
-                                int32_t initial_bound, int32_t* best, int32_t* best_sequence, void* stream)
+                                int32_t initial_bound, int32_t* best, int32_t* best_sequence,
+                                int32_t* round_best, void* stream)
 {
     if (!ctx || !inst || !seeds || num_beams < 1 || iterations < 1) return BSJ_ERR_INVALID;
+    if (inst->n < 1 || inst->m < 1) return BSJ_ERR_INVALID;
+    // ICH/PMS ranks srand() once and draw on from round to round (cpu/v1_pms/main.cpp:56-67)
+    const bool carry = (mode == BSJ_MODE_ICH || mode == BSJ_MODE_PMS);
+    std::vector<RandCarry> rng(carry ? num_beams : 0);
+    for (int b = 0; b < (int)rng.size(); b++) glibc_rand_state(seeds[b], rng[b].r, &rng[b].i);
     int32_t bound = initial_bound;
     int32_t overall = initial_bound;
     std::vector<int32_t> seq((size_t)inst->n * inst->m);
@@ -867,11 +946,13 @@ bsj_status bsj_solve_iterations(bsj_context* ctx, const bsj_instance* inst, int 
     std::vector<std::vector<int32_t>> seqs(num_beams, std::vector<int32_t>(seq.size()));
     for (int it = 0; it < iterations; it++) {
         for (int b = 0; b < num_beams; b++) {
-            beams[b] = bsj_beam{mode, beam_width, bound, seeds[(size_t)it * num_beams + b], 0, 0};
+            const uint32_t seed = carry ? seeds[b] : seeds[(size_t)it * num_beams + b];
+            beams[b] = bsj_beam{mode, beam_width, bound, seed, 0, 0};
             res[b] = bsj_result{};
             res[b].sequence = seqs[b].data();
         }
-        bsj_status s = bsj_solve_batch(ctx, 1, inst, num_beams, beams.data(), res.data(), stream);
+        bsj_status s = solve_batch_impl(ctx, 1, inst, num_beams, beams.data(), res.data(), stream,
+                                        carry ? rng.data() : nullptr, carry ? rng.data() : nullptr);
         if (s != BSJ_OK) return s;
         // MPI_Allreduce(MIN) of the ranks' bests (gpu/v1/main.cu:66-70)
         for (int b = 0; b < num_beams; b++) {
@@ -881,6 +962,7 @@ bsj_status bsj_solve_iterations(bsj_context* ctx, const bsj_instance* inst, int 
             }
         }
         bound = overall;
+        if (round_best) round_best[it] = overall;
     }
     if (best) *best = overall;
     if (best_sequence) {

@@ -1261,14 +1261,19 @@ __device__ __forceinline__ void heap_insert(unsigned long long* hk, uint32_t* hv
     }
 }
 
+// glibc rand() stream: ring[34] holds r[i-34 .. i-1] at index (position mod 34); i is the
+// position of the next value, kept in [34, 68) so that no pass of any length overflows it.
 struct Rng {
     uint32_t* ring;
     uint32_t i;
     __device__ __forceinline__ uint32_t next()
     {
-        uint32_t v = ring[(i - 31u) % 34u] + ring[(i - 3u) % 34u];
-        ring[i % 34u] = v;
-        i++;
+        const uint32_t k = i - 34u;                     // i mod 34
+        const uint32_t a = k + 3u < 34u ? k + 3u : k + 3u - 34u;     // (i - 31) mod 34
+        const uint32_t b = k + 31u < 34u ? k + 31u : k + 31u - 34u;  // (i - 3) mod 34
+        const uint32_t v = ring[a] + ring[b];
+        ring[k] = v;
+        i = (k == 33u) ? 34u : i + 1u;
         return v >> 1;
     }
 };

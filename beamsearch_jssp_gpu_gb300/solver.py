@@ -110,22 +110,33 @@ class Context:
                                 [BeamSpec(mode, beam_width, best_known, seed, 0, -1)], stream)[0]
 
     def solve_iterations(self, machine, duration, mode: str, beam_width: int, seeds,
-                         initial_bound: int = nat.NO_BOUND, stream: int = 0):
-        """Multi-start passes with the bound carried between rounds; ``seeds`` is
-        [iterations, beams].  Returns (best makespan, best sequence)."""
+                         initial_bound: int = nat.NO_BOUND, stream: int = 0, iterations: int = 0):
+        """Multi-start passes with the bound carried between rounds (bsj_solve_iterations).
+
+        Gpu modes: ``seeds`` is ``[iterations, beams]`` random_seeds.  ICH/PMS: ``seeds``
+        is ``[beams]`` srand() seeds whose rand() streams run on across ``iterations``
+        rounds.  Returns (best makespan, best sequence, best after each round)."""
         ia = _InstanceArrays([(machine, duration)])
-        sd = np.ascontiguousarray(seeds, dtype=np.uint32)
-        if sd.ndim != 2:
-            raise ValueError("seeds must be [iterations, beams]")
+        sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.int64) & 0xFFFFFFFF, dtype=np.uint32)
+        carry = nat.MODES[mode] >= nat.MODES["ich"]
+        if carry:
+            if sd.ndim != 1 or iterations < 1:
+                raise ValueError("ICH/PMS: seeds must be [beams] and iterations >= 1")
+            beams, rounds = sd.shape[0], int(iterations)
+        else:
+            if sd.ndim != 2:
+                raise ValueError("seeds must be [iterations, beams]")
+            rounds, beams = sd.shape
         best = ctypes.c_int32()
         n, m = ia.sizes[0]
         seq = np.zeros(n * m, dtype=np.int32)
-        st = self.lib.bsj_solve_iterations(self.h, ia.c, nat.MODES[mode], int(beam_width), sd.shape[1],
-                                           sd.shape[0], sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-                                           int(initial_bound), ctypes.byref(best), _i32p(seq),
+        per_round = np.zeros(rounds, dtype=np.int32)
+        st = self.lib.bsj_solve_iterations(self.h, ia.c, nat.MODES[mode], int(beam_width), beams, rounds,
+                                           sd.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                           int(initial_bound), ctypes.byref(best), _i32p(seq), _i32p(per_round),
                                            ctypes.c_void_p(stream) if stream else None)
         self._check(st)
-        return best.value, seq
+        return best.value, seq, per_round
 
     def plan(self, instances: Sequence, beams: Sequence[BeamSpec]) -> "Plan":
         return Plan(self, instances, beams)
@@ -223,8 +234,9 @@ def solve_batch(instances, beams) -> List[dict]:
     return _ctx().solve_batch(instances, beams)
 
 
-def solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound=nat.NO_BOUND):
-    return _ctx().solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound)
+def solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound=nat.NO_BOUND, iterations=0):
+    return _ctx().solve_iterations(machine, duration, mode, beam_width, seeds, initial_bound,
+                                   iterations=iterations)
 
 
 def _run_ref_style(mode: str, inst: JSSPInstance, beam_width: int, best_known: int, random_seed: int,

@@ -88,6 +88,9 @@ typedef struct bsj_plan bsj_plan;
 const char *bsj_version(void);
 const char *bsj_status_string(bsj_status s);
 
+/* Number of CUDA devices visible to the process (0 with BSJ_ERR_CUDA when there is no
+   usable driver or device). */
+bsj_status bsj_device_count(int32_t *count);
 /* Context on CUDA device `device` (-1 = current device). */
 bsj_status bsj_create(bsj_context **out, int device);
 void bsj_destroy(bsj_context *ctx);
@@ -106,14 +109,21 @@ bsj_status bsj_solve_batch(bsj_context *ctx, int num_instances, const bsj_instan
                            int num_beams, const bsj_beam *beams, bsj_result *results,
                            void *stream);
 
-/* Multi-start driver (gpu/v1/main.cu:62-71 with the MPI ranks as beams): `iterations`
-   rounds of `num_beams` beams; round i's beams use seeds[i*num_beams + b] and, as their
-   pruning bound, the best makespan of all earlier rounds (frozen per round).  Each
-   results entry holds that beam's last round; *best receives the overall best. */
+/* Multi-start driver with the MPI ranks as beams (gpu/v1/main.cu:58-71,
+   cpu/v1_pms/main.cpp:56-67): `iterations` rounds of `num_beams` beams in one launch
+   each; a round's beams take, as their pruning bound, the best makespan of all earlier
+   rounds and initial_bound (the MPI_Allreduce(MIN), frozen per round).
+   Gpu modes: beam b of round i uses random_seed seeds[i*num_beams + b] (what rank b's
+   rand() drew for round i).  ICH/PMS: seeds[b] is rank b's srand() seed and its rand()
+   stream continues from round to round as the process-wide one does; seeds holds
+   num_beams entries.  *best receives the overall best, best_sequence (n*m, may be NULL)
+   the schedule of the first beam that reached it (zeros if none beat initial_bound),
+   round_best[i] (may be NULL) the best after round i. */
 bsj_status bsj_solve_iterations(bsj_context *ctx, const bsj_instance *inst, int mode,
                                 int beam_width, int num_beams, int iterations,
                                 const uint32_t *seeds, int32_t initial_bound,
-                                int32_t *best, int32_t *best_sequence, void *stream);
+                                int32_t *best, int32_t *best_sequence, int32_t *round_best,
+                                void *stream);
 
 /* Plans: the split form of bsj_solve_batch used for device-resident timing.
    bsj_plan_create uploads instances and sizes device memory; bsj_plan_run enqueues every
@@ -138,6 +148,23 @@ bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, double *sele
 bsj_status bsj_plan_set_timing(bsj_plan *plan, int enable);
 bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches, int count);
 
+/* Instance files in the reference's text format (cpu/common/instance_parser.cpp:8-93).
+   bsj_instance_resolve: `arg` as a path, else the reference's Lawrence/Taillard search
+   list; BSJ_ERR_INVALID when nothing is found.  bsj_instance_read: *n, *m from the header;
+   with machine/duration non-NULL also the [n*m] pairs (machines 0-based, as written),
+   BSJ_ERR_LIMIT when n*m > capacity.  A truncated body reads as machine 0 / duration 0,
+   as the reference's fscanf loop leaves it. */
+bsj_status bsj_instance_resolve(const char *arg, char *out_path, int32_t path_size);
+bsj_status bsj_instance_read(const char *path, int32_t *n, int32_t *m, int32_t *machine,
+                             int32_t *duration, int32_t capacity);
+/* Start times of the semi-active schedule a dispatch order denotes: every op starts at
+   max(its machine's ready time, its job predecessor's finish), the rule each search level
+   applies (gpu/common/gpu_snapshot.cuh:47-70).  `sequence` holds the n*m 1-based op ids
+   of a bsj_result; start[op] (0-based op id, may be NULL) and *makespan receive the
+   schedule.  BSJ_ERR_INVALID when the order is not a permutation that keeps every job's
+   steps in order. */
+bsj_status bsj_schedule_decode(const bsj_instance *inst, const int32_t *sequence, int32_t *start,
+                               int32_t *makespan);
 /* Single-beam solve that allocates nothing (no counterpart in the reference).
    For callers that must not allocate device memory -- operator/plugin hosts whose device
    memory is owned and budgeted by the host framework, and latency-critical loops where a

@@ -41,3 +41,11 @@ int run_gpu_beam_search_v1(const JSSPInstance& inst, int beam_width, int best_kn
 // Same contract with gpu/v2_twophases semantics.
 int run_gpu_beam_search_v2(const JSSPInstance& inst, int beam_width, int best_known,
                            int random_seed, int* out_best_sequence = nullptr);
+
+// The instance reader of cpu/common/instance_parser.h:5-9, same signatures and behaviour
+// (instance_parser.cpp:8-34, :37-93): resolve_instance_file tries the argument as a path,
+// then the reference's list of Lawrence/Taillard locations; parse_instance fills `inst`
+// with dummy ops 0 and n*m+1 and 1-based machines, and prints to stderr and returns
+// false when the file cannot be opened or its header read.
+bool resolve_instance_file(const char* input_arg, char* out_path, int path_size);
+bool parse_instance(const char* filepath, JSSPInstance& inst);

@@ -464,7 +464,11 @@ static void beam_reset(obeam *b, opool *pool)
     b->spare = &pool->st[0];
 }
 
-static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int max_levels)
+/* `carry` (may be NULL): the rand() stream to draw from, left where the pass ends, as the
+   process-wide state is between the reference's successive calls (cpu/v1_pms/main.cpp:56,64);
+   NULL seeds a fresh stream with p->seed. */
+static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int max_levels,
+                     grand_t *carry)
 {
     const int N = x->N, K = p->beam_width, mode = p->mode;
     opool pool[2] = {{0}, {0}};
@@ -475,8 +479,9 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
     if (pool_init(&pool[0], x, K + 1) || pool_init(&pool[1], x, K + 1)) goto out;
     if (beam_init(&beam[0], &pool[0], K) || beam_init(&beam[1], &pool[1], K)) goto out;
 
-    grand_t g;
-    grand_seed(&g, p->seed);
+    grand_t own;
+    if (!carry) grand_seed(&own, p->seed);
+    grand_t *gp = carry ? carry : &own;
     int cb = 0;
     /* the initial beam holds the root */
     st_root(x, beam[cb].spare);
@@ -502,7 +507,7 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
                     st_copy(x, child, par);
                     st_erase_at(child, idx);
                     st_schedule(x, child, op);
-                    child->score = (double)child->cmax + (grand_next(&g) % 100) * 0.01;
+                    child->score = (double)child->cmax + (grand_next(gp) % 100) * 0.01;
                     child->lineage = ((uint32_t)c << 8) | (uint32_t)op_job(x, op);
                     res->expanded++;
                     res->slots++;
@@ -511,7 +516,7 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
             } else {
                 int nbr = par->nready;
                 if (nbr <= 0) continue;
-                int pivot = grand_next(&g) % nbr;
+                int pivot = grand_next(gp) % nbr;
                 int target = op_machine1(x, par->ready[pivot]);
                 for (int r = 0; r < nbr; r++) {
                     if (op_machine1(x, par->ready[r]) != target) continue;
@@ -522,7 +527,7 @@ static int solve_cpu(const octx *x, const orc_params *p, orc_result *res, int ma
                         if (child->ready[i] == op) { st_erase_at(child, i); break; }
                     }
                     st_schedule(x, child, op);
-                    double noise = (double)(grand_next(&g) % 1000) / 1000000.0;
+                    double noise = (double)(grand_next(gp) % 1000) / 1000000.0;
                     child->score = ((double)child->cmax / (double)child->nseq) + noise;
                     child->lineage = ((uint32_t)c << 8) | (uint32_t)op_job(x, op);
                     res->expanded++;
@@ -572,8 +577,8 @@ out:
     return rc;
 }
 
-int orc_solve_levels(const orc_instance *inst, const orc_params *p, orc_result *res,
-                     int max_levels)
+static int solve_any(const orc_instance *inst, const orc_params *p, orc_result *res,
+                     int max_levels, grand_t *carry)
 {
     if (!inst || !p || !res) return -1;
     if (inst->n < 1 || inst->m < 1 || inst->n > 255 || p->beam_width < 1) return -2;
@@ -593,10 +598,64 @@ int orc_solve_levels(const orc_instance *inst, const orc_params *p, orc_result *
         return solve_gpu(&x, p, res, max_levels);
     case ORC_ICH:
     case ORC_PMS:
-        return solve_cpu(&x, p, res, max_levels);
+        return solve_cpu(&x, p, res, max_levels, carry);
     default:
         return -4;
     }
+}
+
+int orc_solve_levels(const orc_instance *inst, const orc_params *p, orc_result *res,
+                     int max_levels)
+{
+    return solve_any(inst, p, res, max_levels, NULL);
+}
+
+/* Multi-start loop of the reference drivers with the MPI ranks as beams: gpu/v1/main.cu:58-71
+   (each rank draws a random_seed per round, calls the solver with the all-reduced bound,
+   then MPI_Allreduce(MIN)) and cpu/v1_pms/main.cpp:56-67 (srand once per rank, the rand()
+   stream runs on across rounds). */
+int orc_solve_iterations(const orc_instance *inst, int mode, int K, int num_beams, int iterations,
+                         const uint32_t *seeds, int32_t initial_bound, int32_t *best,
+                         int32_t *best_seq, int32_t *round_best)
+{
+    if (!inst || !seeds || num_beams < 1 || iterations < 1) return -1;
+    const int N = inst->n * inst->m;
+    const int cpu = (mode == ORC_ICH || mode == ORC_PMS);
+    grand_t *streams = (grand_t *)malloc((size_t)num_beams * sizeof(grand_t));
+    int32_t *seq = (int32_t *)malloc((size_t)N * sizeof(int32_t));
+    if (!streams || !seq) { free(streams); free(seq); return -1; }
+    if (cpu)
+        for (int b = 0; b < num_beams; b++) grand_seed(&streams[b], seeds[b]);
+    int32_t overall = initial_bound, bound = initial_bound;
+    int have = 0, rc = 0;
+    for (int it = 0; it < iterations && rc == 0; it++) {
+        for (int b = 0; b < num_beams; b++) {
+            orc_params p;
+            memset(&p, 0, sizeof(p));
+            p.mode = mode;
+            p.beam_width = K;
+            p.best_known = bound;
+            p.seed = cpu ? seeds[b] : seeds[(size_t)it * num_beams + b];
+            orc_result r;
+            memset(&r, 0, sizeof(r));
+            r.seq = seq;
+            rc = solve_any(inst, &p, &r, 1 << 30, cpu ? &streams[b] : NULL);
+            if (rc != 0) break;
+            if (r.makespan < overall) {
+                overall = r.makespan;
+                if (r.found && best_seq) { memcpy(best_seq, seq, (size_t)N * sizeof(int32_t)); have = 1; }
+            }
+        }
+        bound = overall;
+        if (round_best) round_best[it] = overall;
+    }
+    if (rc == 0) {
+        if (best) *best = overall;
+        if (best_seq && !have) memset(best_seq, 0, (size_t)N * sizeof(int32_t));
+    }
+    free(streams);
+    free(seq);
+    return rc;
 }
 
 int orc_solve(const orc_instance *inst, const orc_params *p, orc_result *res)

@@ -64,6 +64,15 @@ int orc_solve(const orc_instance *inst, const orc_params *p, orc_result *res);
 int orc_solve_levels(const orc_instance *inst, const orc_params *p, orc_result *res,
                      int max_levels);
 
+/* Multi-start loop with the ranks as beams (gpu/v1/main.cu:58-71, cpu/v1_pms/main.cpp:56-67):
+   round it's beams get the best of all earlier rounds as bound.  gpu modes: beam b of round
+   it uses seeds[it*num_beams + b]; ICH/PMS: seeds[b] is rank b's srand() seed and its
+   rand() stream continues from round to round.  round_best[it] (may be NULL) receives the
+   best after round it; best_seq the schedule of the first beam that set the final best. */
+int orc_solve_iterations(const orc_instance *inst, int mode, int K, int num_beams, int iterations,
+                         const uint32_t *seeds, int32_t initial_bound, int32_t *best,
+                         int32_t *best_seq, int32_t *round_best);
+
 /* glibc-compatible rand() stream (restated algorithm), exposed for tests. */
 void orc_glibc_rand_fill(uint32_t seed, int32_t *out, int count);
 

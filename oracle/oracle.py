@@ -94,6 +94,11 @@ def _lib():
         lib.orc_gpu_score.restype = ctypes.c_float
         lib.orc_schedule_makespan.argtypes = [ctypes.POINTER(_Instance), ctypes.POINTER(ctypes.c_int32)]
         lib.orc_schedule_makespan.restype = ctypes.c_int32
+        lib.orc_solve_iterations.argtypes = [
+            ctypes.POINTER(_Instance), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+            ctypes.POINTER(ctypes.c_uint32), ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+        lib.orc_solve_iterations.restype = ctypes.c_int
         _orc = lib
     return _orc
 
@@ -136,6 +141,27 @@ def solve(machine, duration, mode: str, K: int, seed: int, best_known: int = 500
         out["trace"] = tr
         out["trace_count"] = tc
     return out
+
+
+def solve_iterations(machine, duration, mode: str, K: int, seeds, iterations: int,
+                     initial_bound: int = 500000) -> dict:
+    """Multi-start loop with the ranks as beams (orc_solve_iterations).  ``seeds`` is
+    ``[iterations, beams]`` for the gpu modes and ``[beams]`` (srand seeds, the rand()
+    stream carried across rounds) for ICH/PMS.  Returns best, seq and round_best."""
+    mc = np.ascontiguousarray(machine, dtype=np.int32)
+    du = np.ascontiguousarray(duration, dtype=np.int32)
+    n, m = mc.shape
+    sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.int64) & 0xFFFFFFFF, dtype=np.uint32)
+    beams = sd.shape[-1]
+    inst = _Instance(n, m, _ptr(mc), _ptr(du))
+    best = ctypes.c_int32()
+    seq = np.zeros(n * m, dtype=np.int32)
+    rounds = np.zeros(iterations, dtype=np.int32)
+    rc = _lib().orc_solve_iterations(ctypes.byref(inst), MODES[mode], K, beams, iterations, _ptr(sd.ravel()),
+                                     initial_bound, ctypes.byref(best), _ptr(seq), _ptr(rounds))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the input (status {rc})")
+    return dict(best=best.value, seq=seq, round_best=rounds)
 
 
 def glibc_rand(seed: int, count: int) -> np.ndarray:

@@ -51,24 +51,32 @@ def test_beams_sharing_instances(ctx):
         assert r["makespan"] == O.solve(mc, du, bm.mode, bm.beam_width, bm.seed)["makespan"]
 
 
-@pytest.mark.parametrize("mode", ["v1", "v2", "pms"])
+@pytest.mark.parametrize("mode", ["v1", "v2", "clean"])
 def test_iterations_carry_the_bound(ctx, mode):
-    """gpu/v1/main.cu:62-71 with B ranks: every round uses the best of earlier rounds."""
+    """gpu/v1/main.cu:58-71 with 3 ranks: every round uses the best of earlier rounds."""
     mc, du = synthetic_instance(10, 5, 3)
     seeds = np.arange(12, dtype=np.uint32).reshape(4, 3) * 7919 + 11
-    best, seq = ctx.solve_iterations(mc, du, mode, 32, seeds)
-    bound, want_seq = 500000, None
-    for it in range(4):
-        rs = [O.solve(mc, du, mode, 32, int(s), best_known=bound) for s in seeds[it]]
-        new = min([bound] + [r["makespan"] for r in rs])
-        for r in rs:
-            if r["makespan"] == new and r["found"] and new < bound:
-                want_seq = r["seq"]
-                break
-        bound = new
-    assert best == bound
+    best, seq, rounds = ctx.solve_iterations(mc, du, mode, 32, seeds)
+    want = O.solve_iterations(mc, du, mode, 32, seeds, 4)
+    assert best == want["best"]
+    assert np.array_equal(rounds, want["round_best"])
     assert O.schedule_makespan(mc, du, seq) == best
-    assert np.array_equal(seq, want_seq)
+    assert np.array_equal(seq, want["seq"])
+
+
+@pytest.mark.parametrize("mode", ["pms", "ich"])
+@pytest.mark.parametrize("n,m,K,beams,iters", [(10, 5, 32, 3, 4), (20, 10, 64, 2, 3), (15, 15, 128, 4, 2)])
+def test_iterations_continue_the_rand_stream(ctx, mode, n, m, K, beams, iters):
+    """cpu/v1_pms/main.cpp:56-67: each rank seeds rand() once and its later rounds draw
+    on from where the previous pass stopped."""
+    mc, du = synthetic_instance(n, m, 5)
+    seeds = np.arange(beams, dtype=np.uint32) * 104729 + 3
+    best, seq, rounds = ctx.solve_iterations(mc, du, mode, K, seeds, iterations=iters)
+    want = O.solve_iterations(mc, du, mode, K, seeds, iters)
+    assert best == want["best"]
+    assert np.array_equal(rounds, want["round_best"])
+    if best < 500000:
+        assert O.schedule_makespan(mc, du, seq) == best
 
 
 def test_plan_rerun_is_deterministic(ctx):

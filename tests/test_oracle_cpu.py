@@ -65,6 +65,39 @@ def test_oracle_pms_larger_matches_reference(tmp_path):
         assert O.solve(mc, du, "pms", 256, seed)["makespan"] == O.ref_pms(path, 256, 500000, seed)
 
 
+@needs_ref
+def test_oracle_pms_iterations_match_reference(tmp_path):
+    # srand once, then rounds that continue the rand() stream with the carried bound
+    # (cpu/v1_pms/main.cpp:56-67 with one rank)
+    for (n, m, iseed, K) in ((8, 4, 3, 16), (12, 6, 5, 32), (15, 10, 1, 64)):
+        mc, du = synthetic_instance(n, m, iseed)
+        path = str(tmp_path / f"i{iseed}.txt")
+        write_instance(path, mc, du)
+        for seed in (0, 11):
+            for iters in (1, 2, 5):
+                got = O.solve_iterations(mc, du, "pms", K, [seed], iters)
+                assert got["best"] == O.ref_pms_iterations(path, K, seed, iters), (n, m, seed, iters)
+                assert O.schedule_makespan(mc, du, got["seq"]) == got["best"]
+
+
+def test_oracle_iterations_compose_single_solves():
+    # gpu modes: round r's beams are independent solves bounded by the earlier rounds' best
+    mc, du = synthetic_instance(10, 5, 2)
+    seeds = np.array([[3, 9], [4, 10], [5, 11]], dtype=np.uint32)
+    for mode in ("v1", "v2", "clean"):
+        got = O.solve_iterations(mc, du, mode, 32, seeds, 3)
+        bound = 500000
+        for it in range(3):
+            spans = [O.solve(mc, du, mode, 32, int(seeds[it, b]), best_known=bound)["makespan"] for b in range(2)]
+            bound = min([bound] + spans)
+            assert got["round_best"][it] == bound, (mode, it)
+        assert got["best"] == bound
+    # ICH/PMS: the first round equals plain solves with the srand seeds
+    for mode in ("ich", "pms"):
+        got = O.solve_iterations(mc, du, mode, 32, [7, 8], 1)
+        assert got["best"] == min(O.solve(mc, du, mode, 32, s)["makespan"] for s in (7, 8))
+
+
 @pytest.mark.parametrize("mode", ["ich", "pms", "v1", "v2", "clean"])
 def test_oracle_schedules_verify(mode):
     for iseed in range(3):
