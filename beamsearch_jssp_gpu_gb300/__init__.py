@@ -9,7 +9,7 @@ branching mode and seed.  One search level runs as hand-written sm_103a CUDA ker
 from .instance import (JSSPInstance, Operation, format_instance, parse_instance,  # noqa: F401
                        resolve_instance_file, schedule_makespan, synthetic_instance,
                        write_instance)
-from .solver import (BeamSpec, Context, Plan, beam_search_ich, beam_search_pms,  # noqa: F401
+from .solver import (BeamSpec, Context, Plan, Server, beam_search_ich, beam_search_pms,  # noqa: F401
                      run_gpu_beam_search_v1, run_gpu_beam_search_v2, solve, solve_batch,
                      solve_iterations)
 from ._native import BsjError, NO_BOUND, MODES  # noqa: F401

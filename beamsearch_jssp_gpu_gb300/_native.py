@@ -31,7 +31,25 @@ EXPORTED = [
     "bsj_plan_results", "bsj_plan_destroy", "bsj_plan_launches", "bsj_plan_stats",
     "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_solve_noalloc",
     "bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count",
+    "bsj_plan_estimate", "bsj_plan_device_bytes", "bsj_plan_update",
+    "bsj_server_create", "bsj_server_destroy", "bsj_submit", "bsj_poll", "bsj_wait", "bsj_server_get_stats",
 ]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("max_inflight", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("memory_budget", ctypes.c_int64)]
+
+
+class RequestTimes(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "plans_built", "plans_reused",
+                                               "peak_inflight", "peak_device_bytes", "budget_bytes",
+                                               "pending")] + \
+               [(k, ctypes.c_double) for k in ("build_ms", "update_ms", "launch_ms", "collect_ms")]
 
 
 class BsjError(RuntimeError):
@@ -113,6 +131,21 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_schedule_decode.argtypes = [P(Instance), P(ctypes.c_int32), P(ctypes.c_int32),
                                       P(ctypes.c_int32)]
     L.bsj_device_count.argtypes = [P(ctypes.c_int32)]
+    L.bsj_plan_estimate.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam), P(ctypes.c_int64)]
+    L.bsj_plan_device_bytes.argtypes = [vp]
+    L.bsj_plan_device_bytes.restype = ctypes.c_int64
+    L.bsj_plan_update.argtypes = [vp, ctypes.c_int, P(Instance), ctypes.c_int, P(Beam)]
+    # serving (continuous batching)
+    L.bsj_server_create.argtypes = [P(vp), ctypes.c_int, P(ServerConfig)]
+    L.bsj_server_destroy.argtypes = [vp]
+    L.bsj_server_destroy.restype = None
+    L.bsj_submit.argtypes = [vp, P(Instance), P(Beam), P(ctypes.c_uint64)]
+    L.bsj_poll.argtypes = [vp, ctypes.c_uint64, P(Result), P(RequestTimes), P(ctypes.c_int32)]
+    L.bsj_wait.argtypes = [vp, ctypes.c_uint64, P(Result), P(RequestTimes)]
+    L.bsj_server_get_stats.argtypes = [vp, P(ServerStats)]
+    for name in ("bsj_plan_estimate", "bsj_plan_update", "bsj_server_create", "bsj_submit", "bsj_poll",
+                 "bsj_wait", "bsj_server_get_stats"):
+        getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count"):
         getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libbsj.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
-SOURCES = ["bsj_kernels.cu", "bsj_engine.cu", "bsj_compat.cpp", "bsj_noalloc.cu", "bsj_instance.cpp"]
+SOURCES = ["bsj_kernels.cu", "bsj_engine.cu", "bsj_compat.cpp", "bsj_noalloc.cu", "bsj_instance.cpp",
+           "bsj_server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr"]

@@ -69,6 +69,7 @@ struct bsj_plan {
     std::vector<int32_t> cprefix;
     std::vector<int32_t> group_init;
     std::vector<int32_t> seg_group;
+    std::string shape;  // shape_key() of the batch the plan was built for
     // device
     void* mem = nullptr;
     size_t mem_bytes = 0;
@@ -170,10 +171,14 @@ bsj_status ensure_arena(bsj_context* ctx, size_t bytes)
     return BSJ_OK;
 }
 
+std::string shape_key(int ninst, const bsj_instance* insts, int nbeams, const bsj_beam* beams);
+
+// With `bytes_only` non-null, computes the plan's device footprint into it and allocates
+// nothing (*out is left untouched).
 bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, int nbeams,
-                      const bsj_beam* beams, bool use_arena, bsj_plan** out)
+                      const bsj_beam* beams, bool use_arena, bsj_plan** out, size_t* bytes_only = nullptr)
 {
-    if (!ctx || !out || ninst < 1 || nbeams < 1 || !insts || !beams)
+    if (!ctx || (!out && !bytes_only) || ninst < 1 || nbeams < 1 || !insts || !beams)
         return fail(ctx, BSJ_ERR_INVALID, "plan: null argument or empty batch");
     for (int i = 0; i < ninst; i++) {
         bsj_status s = validate_instance(ctx, insts[i]);
@@ -183,6 +188,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     p->ctx = ctx;
     p->nseg = nbeams;
     p->ninst = ninst;
+    p->shape = shape_key(ninst, insts, nbeams, beams);
 
     // op tables: (duration << 8) | machine
     std::vector<uint32_t> ops;
@@ -326,6 +332,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     p->mem_bytes = o;
     p->beam_bytes = off_beam;
     p->slot_bytes = off_slot;
+    if (bytes_only) {
+        *bytes_only = o;
+        delete p;
+        return BSJ_OK;
+    }
 
     if (use_arena) {
         bsj_status s = ensure_arena(ctx, o);
@@ -716,6 +727,28 @@ bsj_status bsj_plan_create(bsj_context* ctx, int num_instances, const bsj_instan
     if (!ctx) return BSJ_ERR_INVALID;
     cudaSetDevice(ctx->device);
     return plan_build(ctx, num_instances, instances, num_beams, beams, false, out);
+}
+
+bsj_status bsj_plan_estimate(bsj_context* ctx, int num_instances, const bsj_instance* instances,
+                             int num_beams, const bsj_beam* beams, int64_t* device_bytes)
+{
+    if (!ctx || !device_bytes) return BSJ_ERR_INVALID;
+    size_t bytes = 0;
+    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, false, nullptr, &bytes);
+    if (s == BSJ_OK) *device_bytes = (int64_t)bytes;
+    return s;
+}
+
+int64_t bsj_plan_device_bytes(const bsj_plan* p) { return p ? (int64_t)p->mem_bytes : 0; }
+
+bsj_status bsj_plan_update(bsj_plan* p, int num_instances, const bsj_instance* instances, int num_beams,
+                           const bsj_beam* beams)
+{
+    if (!p || !instances || !beams || num_instances != p->ninst || num_beams != p->nseg) return BSJ_ERR_INVALID;
+    if (p->shape != shape_key(num_instances, instances, num_beams, beams))
+        return fail(p->ctx, BSJ_ERR_INVALID, "plan update: sizes, modes, widths or groups differ from the plan's");
+    cudaSetDevice(p->ctx->device);
+    return plan_refresh(p, num_instances, instances, beams);
 }
 
 bsj_status bsj_plan_run(bsj_plan* p, void* stream)

@@ -13,6 +13,8 @@
 //
 // Integer work only, apart from the fp32 (gpu modes) / fp64 (PMS) score, computed with
 // the reference's operations in its order.
+#include <mutex>
+
 #include "bsj_kernels.h"
 
 namespace bsj {
@@ -1489,23 +1491,10 @@ static cudaError_t set_carveout()
     return e;
 }
 
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n)
-{
-    cudaError_t ec = set_carveout();
-    if (ec != cudaSuccess) return ec;
-    cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)select_smem_bytes(sort_cap));
-
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_heap, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)heap_smem_bytes(max_k, stage_bytes));
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem_bytes(sb_max, max_n));
-}
+// The dynamic shared-memory limit is an attribute of the kernel, shared by every plan,
+// context and thread of the process, and graphs captured earlier launch with the sizes
+// they were captured with: limits are only ever raised, under one lock.
+static std::mutex g_attr_mu;
 
 template <typename F>
 static cudaError_t raise_smem(F* fn, size_t bytes)
@@ -1517,15 +1506,26 @@ static cudaError_t raise_smem(F* fn, size_t bytes)
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n)
+{
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    cudaError_t e = set_carveout();
+    if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_heap, heap_smem_bytes(max_k, stage_bytes));
+    if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
+    return e;
+}
+
 cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
 {
+    std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e != cudaSuccess) return e;
-    e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
-    if (e != cudaSuccess) return e;
-    e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
-    if (e != cudaSuccess) return e;
-    return raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
+    return e;
 }
 
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)

@@ -18,7 +18,7 @@ from . import _native as nat
 from .instance import JSSPInstance
 
 __all__ = ["Context", "Plan", "BeamSpec", "run_gpu_beam_search_v1", "run_gpu_beam_search_v2",
-           "beam_search_ich", "beam_search_pms", "solve", "solve_batch", "solve_iterations"]
+           "beam_search_ich", "beam_search_pms", "solve", "solve_batch", "solve_iterations", "Server"]
 
 
 def _i32p(a: np.ndarray):
@@ -141,6 +141,14 @@ class Context:
     def plan(self, instances: Sequence, beams: Sequence[BeamSpec]) -> "Plan":
         return Plan(self, instances, beams)
 
+    def estimate(self, instances: Sequence, beams: Sequence[BeamSpec]) -> int:
+        """Device bytes a plan of this batch would hold (bsj_plan_estimate)."""
+        ia = _InstanceArrays(instances)
+        cb = (nat.Beam * len(beams))(*[b.to_c() for b in beams])
+        out = ctypes.c_int64()
+        self._check(self.lib.bsj_plan_estimate(self.h, len(ia.arrays), ia.c, len(beams), cb, ctypes.byref(out)))
+        return int(out.value)
+
 
 class Plan:
     """A prepared batch (``bsj_plan_*``): inputs uploaded once, runs enqueued on a stream."""
@@ -209,6 +217,92 @@ class Plan:
         cnt = (ctypes.c_int64 * 5)()
         self.ctx._check(self.lib.bsj_plan_kernel_ms(self.h, ms, cnt, 5))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNELS)}
+
+
+class Server:
+    """Continuous-batching request loop on one GPU (include/bsj.h ``bsj_server_*``).
+
+    ``submit`` queues one solve and returns a ticket at once; the server admits queued
+    requests while an in-flight slot and the memory budget allow, runs them concurrently
+    and reuses plans by shape.  ``poll`` / ``wait`` return the result dict with
+    ``queue_ms`` and ``run_ms``.  Thread-safe."""
+
+    def __init__(self, device: int = 0, max_inflight: int = 0, memory_budget: int = 0):
+        self.lib = nat.load()
+        h = ctypes.c_void_p()
+        cfg = nat.ServerConfig(int(max_inflight), 0, int(memory_budget))
+        st = self.lib.bsj_server_create(ctypes.byref(h), int(device), ctypes.byref(cfg))
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, "cannot create the server")
+        self.h = h
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bsj_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, machine, duration, mode: str = "v2", beam_width: int = 1024, seed: int = 0,
+               best_known: int = nat.NO_BOUND) -> int:
+        mc = np.ascontiguousarray(machine, dtype=np.int32)
+        du = np.ascontiguousarray(duration, dtype=np.int32)
+        n, m = mc.shape
+        inst = nat.Instance(n, m, _i32p(mc), _i32p(du))
+        beam = BeamSpec(mode, beam_width, best_known, seed).to_c()
+        t = ctypes.c_uint64()
+        st = self.lib.bsj_submit(self.h, ctypes.byref(inst), ctypes.byref(beam), ctypes.byref(t))
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, "request rejected")
+        self._n[t.value] = n * m
+        return t.value
+
+    def _finish(self, ticket, st, res, seq, times) -> dict:
+        self._n.pop(ticket, None)
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, f"request {ticket} failed")
+        d = _result_dict(res, seq)
+        d["queue_ms"] = times.queue_ms
+        d["run_ms"] = times.run_ms
+        return d
+
+    def poll(self, ticket: int) -> Optional[dict]:
+        seq = np.zeros(self._n.get(ticket, 1), dtype=np.int32)
+        res = nat.Result()
+        res.sequence = _i32p(seq)
+        times = nat.RequestTimes()
+        done = ctypes.c_int32()
+        st = self.lib.bsj_poll(self.h, ctypes.c_uint64(ticket), ctypes.byref(res), ctypes.byref(times),
+                               ctypes.byref(done))
+        if st == nat.BSJ_OK and not done.value:
+            return None
+        return self._finish(ticket, st, res, seq, times)
+
+    def wait(self, ticket: int) -> dict:
+        seq = np.zeros(self._n.get(ticket, 1), dtype=np.int32)
+        res = nat.Result()
+        res.sequence = _i32p(seq)
+        times = nat.RequestTimes()
+        st = self.lib.bsj_wait(self.h, ctypes.c_uint64(ticket), ctypes.byref(res), ctypes.byref(times))
+        return self._finish(ticket, st, res, seq, times)
+
+    def stats(self) -> dict:
+        s = nat.ServerStats()
+        st = self.lib.bsj_server_get_stats(self.h, ctypes.byref(s))
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, "stats")
+        return {k: (float if t is ctypes.c_double else int)(getattr(s, k)) for k, t in nat.ServerStats._fields_}
 
 
 def _result_dict(r: nat.Result, seq) -> dict:

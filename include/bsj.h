@@ -131,6 +131,17 @@ bsj_status bsj_solve_iterations(bsj_context *ctx, const bsj_instance *inst, int 
 bsj_status bsj_plan_create(bsj_context *ctx, int num_instances, const bsj_instance *instances,
                            int num_beams, const bsj_beam *beams, bsj_plan **out);
 bsj_status bsj_plan_run(bsj_plan *plan, void *stream);
+/* Device bytes bsj_plan_create would allocate for this batch (nothing is allocated);
+   errors as bsj_plan_create.  Serving loops admit work against a memory budget with it. */
+bsj_status bsj_plan_estimate(bsj_context *ctx, int num_instances, const bsj_instance *instances,
+                             int num_beams, const bsj_beam *beams, int64_t *device_bytes);
+/* Device bytes a plan holds. */
+int64_t bsj_plan_device_bytes(const bsj_plan *plan);
+/* New instance data, seeds and bounds into an existing plan, whose captured graph then
+   replays without rebuilding: sizes, modes, widths and bound groups must equal the plan's
+   (BSJ_ERR_INVALID otherwise).  Not while a run of the plan is in flight. */
+bsj_status bsj_plan_update(bsj_plan *plan, int num_instances, const bsj_instance *instances,
+                           int num_beams, const bsj_beam *beams);
 bsj_status bsj_plan_results(bsj_plan *plan, bsj_result *results);
 void bsj_plan_destroy(bsj_plan *plan);
 /* Kernel launches one bsj_plan_run enqueues. */
@@ -165,6 +176,54 @@ bsj_status bsj_instance_read(const char *path, int32_t *n, int32_t *m, int32_t *
    steps in order. */
 bsj_status bsj_schedule_decode(const bsj_instance *inst, const int32_t *sequence, int32_t *start,
                                int32_t *makespan);
+/* ---- Serving: continuous batching of independent solves on one GPU ----
+   The reference solves one instance per synchronous call.  A server takes requests from
+   any number of threads (bsj_submit returns at once), admits queued requests in arrival
+   order while an in-flight slot (a CUDA stream) is free and the device memory their plans
+   would hold fits the budget, runs each as one CUDA-graph launch so that requests overlap
+   on the device, and reuses finished plans for later requests of the same shape.  Each
+   request is one beam (bound_group is ignored); its result equals bsj_solve's. */
+typedef struct bsj_server bsj_server;
+typedef struct {
+    int32_t max_inflight;    /* requests on the device at once; 0 = 32, at most 256 */
+    int32_t reserved;
+    int64_t memory_budget;   /* device bytes held by running and idle plans; 0 = 3/4 of
+                                the free memory at creation */
+} bsj_server_config;
+typedef struct {
+    double queue_ms;         /* submit -> admission */
+    double run_ms;           /* admission -> completion seen by the server */
+} bsj_request_times;
+typedef struct {
+    int64_t submitted, completed;
+    int64_t plans_built, plans_reused;
+    int64_t peak_inflight;
+    int64_t peak_device_bytes;
+    int64_t budget_bytes;
+    int64_t pending;
+    /* host time the server's worker spent, summed over requests (ms): building new plans
+       (allocation + graph capture on first run), loading requests into reused plans,
+       launching, and collecting results */
+    double build_ms, update_ms, launch_ms, collect_ms;
+} bsj_server_stats;
+/* cfg may be NULL (defaults). */
+bsj_status bsj_server_create(bsj_server **out, int device, const bsj_server_config *cfg);
+/* Drops queued requests, waits for running ones, frees everything. */
+void bsj_server_destroy(bsj_server *server);
+/* Copies the request and queues it.  BSJ_ERR_INVALID / BSJ_ERR_LIMIT as bsj_solve would
+   return them, and BSJ_ERR_LIMIT when the request alone exceeds the memory budget. */
+bsj_status bsj_submit(bsj_server *server, const bsj_instance *inst, const bsj_beam *beam,
+                      uint64_t *ticket);
+/* Non-blocking: *done = 0 while the request is queued or running; once *done = 1 the
+   result (the sequence copied into result->sequence when non-NULL), its times and its
+   status are handed out and the ticket is retired.  BSJ_ERR_INVALID for unknown tickets. */
+bsj_status bsj_poll(bsj_server *server, uint64_t ticket, bsj_result *result,
+                    bsj_request_times *times, int32_t *done);
+/* Blocking form of bsj_poll. */
+bsj_status bsj_wait(bsj_server *server, uint64_t ticket, bsj_result *result,
+                    bsj_request_times *times);
+bsj_status bsj_server_get_stats(bsj_server *server, bsj_server_stats *out);
+
 /* Single-beam solve that allocates nothing (no counterpart in the reference).
    For callers that must not allocate device memory -- operator/plugin hosts whose device
    memory is owned and budgeted by the host framework, and latency-critical loops where a
