@@ -15,6 +15,14 @@ Arms:
                      (cpu/v1_pms/solver.cpp), as the oracle port pinned to it, one process
                      per beam on the host cores, each step a bounded sample of levels.
 
+Also on the JSON line (rank 0; --no-extras skips them):
+  "batched"  256 synthetic instances of uneven size (n in {10..100}, m in {5..20},
+             K in {256..4096}) in one bsj_solve_batch, solves/s against the same
+             instances solved one call at a time (the plain path), makespans compared;
+  "serving"  400 requests with Poisson arrivals at 1000/s through bsj_server
+             (continuous batching), solves/s and p50/p99 latency against the plain path
+             on the same requests, results compared.
+
 Multi-GPU: replicas only (each rank runs its own 8 beams; no collective on the data
 path); value = all ranks' candidates / max-over-ranks time.
 """
@@ -289,6 +297,11 @@ def gpu_arm(args) -> int:
                 "peak_source": peaks["source"],
                 "kernel_share": {k: v[0] / max(1e-9, sum(x[0] for x in kms.values())) for k, v in kms.items()}}
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["batched"] = batched_stream(ctx)
+        extras["serving"] = served_stream(ctx, local)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -298,13 +311,99 @@ def gpu_arm(args) -> int:
                 "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk,
                 "select_fallback_levels": stats["select_fallbacks"],
-                "makespans": [r["makespan"] for r in res]}
+                "makespans": [r["makespan"] for r in res], **extras}
         print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+# ------------------------------------------------------------------------------------
+# Batched and served streams (rank 0, after the headline measurement)
+# ------------------------------------------------------------------------------------
+def batched_stream(ctx, count: int = 256, seed: int = 1) -> dict:
+    """256 synthetic instances of uneven size in one set of launches (bsj_solve_batch),
+    against the plain path: the same instances solved one call at a time (bsj_solve)."""
+    import random
+
+    from beamsearch_jssp_gpu_gb300 import BeamSpec, synthetic_instance
+
+    rng = random.Random(seed)
+    insts, beams = [], []
+    for i in range(count):
+        n = rng.choice([10, 15, 20, 30, 50, 100])
+        m = rng.choice([5, 10, 15, 20])
+        K = rng.choice([256, 512, 1024, 4096])
+        insts.append(synthetic_instance(n, m, 10000 + i))
+        beams.append(BeamSpec("v2", K, 500000, rng.randrange(1 << 30), i, -1))
+    ctx.solve_batch(insts, beams)                      # builds and caches the batch plan
+    t0 = time.perf_counter()
+    out = ctx.solve_batch(insts, beams)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plain = [ctx.solve(mc, du, b.mode, b.beam_width, b.seed) for (mc, du), b in zip(insts, beams)]
+    t_plain = time.perf_counter() - t0
+    same = all(a["makespan"] == b["makespan"] and a["expanded"] == b["expanded"] for a, b in zip(out, plain))
+    return {"workload": f"{count} instances, n in {{10,15,20,30,50,100}}, m in {{5,10,15,20}}, "
+                        f"K in {{256,512,1024,4096}}, gpu-v2 mode, one batch of launches",
+            "solves_per_s": count / t_batch, "plain_solves_per_s": count / t_plain,
+            "speedup_vs_plain": t_plain / t_batch, "identical_makespans": same,
+            "expanded_per_s": sum(r["expanded"] for r in out) / t_batch}
+
+
+def served_stream(ctx, device: int, count: int = 400, rate: float = 1000.0, inflight: int = 48,
+                  seed: int = 5) -> dict:
+    """Open-loop Poisson arrivals served by bsj_server (continuous batching), against the
+    plain path solving the same requests one at a time."""
+    import random
+
+    import numpy as np
+
+    from beamsearch_jssp_gpu_gb300 import Server, synthetic_instance
+
+    rng = random.Random(seed)
+    reqs = []
+    for i in range(count):
+        n = rng.choice([15, 20, 30, 50, 100])
+        m = rng.choice([15, 20])
+        K = rng.choice([256, 1024, 4096])
+        mode = rng.choice(["v2", "clean"])
+        mc, du = synthetic_instance(n, m, 20000 + i)
+        reqs.append((mc, du, mode, K, rng.randrange(1 << 30)))
+    t0 = time.perf_counter()
+    plain = [ctx.solve(*r) for r in reqs]
+    t_plain = time.perf_counter() - t0
+    with Server(device, max_inflight=inflight) as srv:
+        # warm the plan pool: a burst of every shape, as a long-running server has
+        shapes = {}
+        for r in reqs:
+            shapes.setdefault((r[0].shape, r[2], r[3]), []).append(r)
+        warm = [srv.submit(*r) for v in shapes.values() for r in v[:4]]
+        for t in warm:
+            srv.wait(t)
+        gaps = np.random.default_rng(seed).exponential(1.0 / rate, count)
+        tickets = []
+        t0 = time.perf_counter()
+        arrival = t0
+        for r, g in zip(reqs, gaps):
+            arrival += g
+            while time.perf_counter() < arrival:
+                pass
+            tickets.append(srv.submit(*r))
+        got = [srv.wait(t) for t in tickets]
+        span = time.perf_counter() - t0
+        st = srv.stats()
+    lat = np.array([g["queue_ms"] + g["run_ms"] for g in got])
+    same = all(a["makespan"] == b["makespan"] and np.array_equal(a["seq"], b["seq"]) for a, b in zip(plain, got))
+    return {"workload": f"{count} requests, Poisson arrivals at {rate:g}/s, n in {{15,20,30,50,100}}, m in "
+                        f"{{15,20}}, K in {{256,1024,4096}}, gpu-v2/clean modes, {inflight} slots",
+            "solves_per_s": count / span, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "plain_solves_per_s": count / t_plain,
+            "speedup_vs_plain": (count / span) / (count / t_plain), "identical_results": same,
+            "plans_built": st["plans_built"], "plans_reused": st["plans_reused"],
+            "peak_inflight": st["peak_inflight"]}
 
 
 def main() -> int:
@@ -314,6 +413,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and served streams")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
