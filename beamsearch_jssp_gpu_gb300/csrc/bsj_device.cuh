@@ -35,9 +35,13 @@ constexpr int kMaxBeam = 16384;
 constexpr int kMaxDuration = (1 << 24) - 1;
 constexpr int kSentinel = 500000;              // "no bound", gpu/v1/main.cu:57
 constexpr int kWarpsPerStepCta = 8;
-constexpr int kChunk = 32;                                 // ranks per k_step work unit
-constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;   // 4
-constexpr int kMaxChunks = kMaxBeam / kChunk;              // 512
+#ifndef BSJ_STEP_CHUNK
+#define BSJ_STEP_CHUNK 32
+#endif
+constexpr int kChunk = BSJ_STEP_CHUNK;                     // ranks per k_step work unit (8..32)
+constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;
+constexpr int kMaxChunks = kMaxBeam / kChunk;
+static_assert(kChunk % kWarpsPerStepCta == 0 && kChunk <= 32, "a chunk is 1..4 ranks per warp");
 constexpr int kSelectThreads = 1024;
 constexpr int kHeapThreads = 64;
 

@@ -451,14 +451,14 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int 
         if (!compat) {
             // rank-ordered prefix of the staged counts, then coalesced copy-out
             if (warp == 0) {
-                const int v = s_nv[lane];
+                const int v = lane < kChunk ? s_nv[lane] : 0;
                 int x = v;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const int y = __shfl_up_sync(FULL_MASK, x, o);
                     if (lane >= o) x += y;
                 }
-                s_pre[lane] = x - v;
+                if (lane < kChunk) s_pre[lane] = x - v;
                 if (lane == 31) s_kcnt = x;
             }
             __syncthreads();
@@ -832,6 +832,84 @@ __device__ int compact_stable(Get get, int V, Keep keep, unsigned long long* dst
     return total;
 }
 
+// 3b. dense ranks.  The survivors of a level carry few distinct scores (~150-250 at
+// 50x20, K=4096: scores are cmax/ns plus a noise of a few ulps) spread over ~2^20 ulps,
+// so their score bits are replaced by the rank of the score among the distinct survivor
+// scores -- strictly monotone, so the (score, slot) order is unchanged -- and the radix
+// sort below needs one 8-bit pass (two above 256 distinct scores) instead of three.
+// Distinct scores are marked in a bitmap over the occupied buckets <= T (2^shift bits
+// each); a popcount prefix over the bitmap words gives each score's rank.  Returns false,
+// keys untouched, when the bitmap would not fit.  Uses the staging area above the first
+// kLsdMax keys (the radix sort's second buffer) for the bitmap, its prefix and the
+// occupied-bucket index.
+constexpr int kDenseOccOff = kLsdMax;              // u16[kNB] occupied-bucket index
+constexpr int kDenseBmOff = kLsdMax + kNB / 4;     // u32[kDenseWords] bitmap, then its prefix
+constexpr int kDenseWords = 4096;
+static_assert(kDenseBmOff + kDenseWords <= kStageKeys, "dense-rank tables exceed the staging area");
+
+__device__ bool dense_rank_keys(unsigned long long* A, int count, int T, int shift, uint32_t smin,
+                                const SelSmem& S)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int W = shift > 5 ? 1 << (shift - 5) : 1;   // bitmap words per occupied bucket
+    const uint32_t omask = (1u << shift) - 1u;
+    uint16_t* occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
+    uint32_t* bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
+    uint32_t* wp = bm + kDenseWords;
+    int* wsum = reinterpret_cast<int*>(S.red);
+    constexpr int BPT = kNB / kSelectThreads;
+    int f[BPT], sum = 0;
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        const int b = tid * BPT + u;
+        f[u] = (b <= T && S.hist[b] != 0u) ? 1 : 0;
+        sum += f[u];
+    }
+    int O;
+    int base = block_exclusive_scan(sum, &O, wsum);
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        occ[tid * BPT + u] = (uint16_t)base;
+        base += f[u];
+    }
+    const int nw = O * W;
+    if (nw > kDenseWords) return false;   // O is the same in every thread
+    for (int w = tid; w < nw; w += nthr) bm[w] = 0u;
+    __syncthreads();
+    for (int i = tid; i < count; i += nthr) {
+        const uint32_t d = (uint32_t)(A[i] >> 32) - smin;
+        const uint32_t off = d & omask;
+        atomicOr(&bm[(int)occ[d >> shift] * W + (int)(off >> 5)], 1u << (off & 31u));
+    }
+    __syncthreads();
+    const int per = (nw + nthr - 1) / nthr;
+    int c = 0;
+    for (int k = 0; k < per; k++) {
+        const int w = tid * per + k;
+        if (w < nw) c += __popc(bm[w]);
+    }
+    int D;
+    int pre = block_exclusive_scan(c, &D, wsum);
+    for (int k = 0; k < per; k++) {
+        const int w = tid * per + k;
+        if (w < nw) {
+            wp[w] = (uint32_t)pre;
+            pre += __popc(bm[w]);
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < count; i += nthr) {
+        const unsigned long long k = A[i];
+        const uint32_t d = (uint32_t)(k >> 32) - smin;
+        const uint32_t off = d & omask;
+        const int w = (int)occ[d >> shift] * W + (int)(off >> 5);
+        const uint32_t rank = wp[w] + (uint32_t)__popc(bm[w] & ((1u << (off & 31u)) - 1u));
+        A[i] = ((unsigned long long)rank << 32) | (k & 0xFFFFFFFFull);
+    }
+    __syncthreads();
+    return true;
+}
+
 // 4. stable LSD radix sort of `count` (<= kLsdMax) keys by their score bits, first R out.
 // Elements p = warp*32*E + e*32 + lane are ranked in element order against per-warp
 // 16-bit digit counters with bit-ballot peer masks (no atomics); a digit-major prefix over
@@ -1106,8 +1184,9 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
         unsigned long long* dst = S.A;
         const int T = S.misc[2], shift = S.misc[4];
         const uint32_t smin = (uint32_t)S.misc[1];
+        const bool bucketed = count <= kLsdMax;   // survivors = the keys of buckets <= T
         __syncthreads();
-        if (count <= kLsdMax) {
+        if (bucketed) {
             const uint32_t lim = ((uint32_t)T + 1u) << shift;  // bucket <= T
             auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
             count = staged ? compact_stable(get_s, V, keep, dst, kLsdMax, S)
@@ -1129,6 +1208,8 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
         }
         const int RR = R < count ? R : count;
         if (count <= kLsdMax) {
+            // bucket counts are intact on the bucketed path (the radix path reuses them)
+            if (bucketed) dense_rank_keys(dst, count, T, shift, smin, S);
             const int E = (count + kSelectThreads - 1) / kSelectThreads;
             unsigned long long* B = S.stg;
             switch (E) {
@@ -1165,14 +1246,24 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     const SegDesc& d = a.segs[seg];
     if (d.mode > MODE_CLEAN || s >= d.N) return;
     SegState& st = a.st[seg];
-    // candidate counts of the level's chunks -> prefix, V
+    // candidate counts of the level's chunks -> prefix, V (up to 2 chunks per thread)
+    constexpr int CPT = (kMaxChunks + kSelectThreads - 1) / kSelectThreads;
     const int nch = (d.K + kChunk - 1) / kChunk;
-    const int c = threadIdx.x;
-    const int v = (c < nch) ? a.kcnt[d.kcnt_off + c] : 0;
+    const int c0 = threadIdx.x * CPT;
+    int cv[CPT], v = 0;
+#pragma unroll
+    for (int u = 0; u < CPT; u++) {
+        cv[u] = (c0 + u < nch) ? a.kcnt[d.kcnt_off + c0 + u] : 0;
+        v += cv[u];
+    }
     int V;
-    const int pre = block_exclusive_scan(v, &V, s_wsum);
-    if (c < nch) s_cpref[c] = pre;
-    if (c == 0) s_cpref[nch] = V;
+    int pre = block_exclusive_scan(v, &V, s_wsum);
+#pragma unroll
+    for (int u = 0; u < CPT; u++) {
+        if (c0 + u < nch) s_cpref[c0 + u] = pre;
+        pre += cv[u];
+    }
+    if (threadIdx.x == 0) s_cpref[nch] = V;
     __syncthreads();
     if (threadIdx.x == 0) {
         st.expanded += V;
