@@ -406,6 +406,56 @@ def served_stream(ctx, device: int, count: int = 400, rate: float = 1000.0, infl
             "peak_inflight": st["peak_inflight"]}
 
 
+def k_sweep(args) -> int:
+    """Time vs beam width on the GPU path (the GPU analogue of cpu/profiling/
+    time_width_study.cpp): 20x15 synthetic instance, gpu-v1 mode, K in {256, 1024, 4096,
+    16384}; per K one beam alone and the four seeds 0-3 as four beams of one launch.
+    One JSON line per (K, beams): ms per search, us per level, expanded candidates/s and
+    the algorithmic bytes per level over the level time."""
+    import torch
+
+    from beamsearch_jssp_gpu_gb300 import BeamSpec, Context, synthetic_instance
+
+    n, m = 20, 15
+    mc, du = synthetic_instance(n, m, 0)
+    ctx = Context(0)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    peaks = _peaks()
+    for K in (256, 1024, 4096, 16384):
+        for nb in (1, 4):
+            plan = ctx.plan([(mc, du)], [BeamSpec("v1", K, 500000, b, 0, -1) for b in range(nb)])
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    plan.run(sh)
+                times = []
+                for _ in range(args.steps):
+                    flush.fill_(1)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    plan.run(sh)
+                    e1.record(stream)
+                    e1.synchronize()
+                    times.append(e0.elapsed_time(e1))
+                st = plan.stats()
+                res = plan.results(with_sequence=False)
+            t = statistics.median(times)
+            levels = n * m
+            alg = st["step_bytes"] + st["select_bytes"]
+            print(json.dumps({"metric": "k-sweep, 20x15, gpu-v1", "beam_width": K, "beams": nb,
+                              "ms_per_search": t, "us_per_level": 1000.0 * t / levels,
+                              "expanded_per_s": st["expanded"] / (t / 1000.0),
+                              "alg_bytes_per_level": alg / levels,
+                              "alg_gbs": alg / (t / 1000.0) / 1e9,
+                              "hbm_frac": alg / (t / 1000.0) / 1e9 / peaks["hbm_gbs"],
+                              "makespans": [r["makespan"] for r in res]}), flush=True)
+            plan.close()
+    ctx.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -414,7 +464,10 @@ def main() -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served streams")
+    ap.add_argument("--k-sweep", action="store_true", help="time vs beam width (20x15, gpu-v1), one line per K")
     args = ap.parse_args()
+    if args.k_sweep:
+        return k_sweep(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)
