@@ -89,7 +89,7 @@ CLI_SRC = os.path.join(HERE, "cli", "bsj_cli.cpp")
 CLI_BIN = os.path.join(OUT_DIR, "bsj_cli")
 # names the reference's Makefile gives its drivers (Makefile:55-95); each is a link to bsj_cli
 CLI_NAMES = ["exec_gpu_v1", "exec_gpu_v2", "exec_gpu_v1_bench", "exec_gpu_v2_bench", "BS-ICH", "BS-PMS",
-             "BS-PMS-bench", "exec_time_width"]
+             "BS-PMS-bench", "exec_cpu_time_width", "exec_time_width"]
 
 
 def build_cli(force: bool = False) -> str:

@@ -6,7 +6,7 @@
 //   BS-ICH                                 cpu/v0_ich/main.cpp:9-55
 //   BS-PMS                                 cpu/v1_pms/main.cpp:10-85
 //   BS-PMS-bench                           cpu/v1_pms/benchmark.cpp:10-83
-//   exec_time_width                        cpu/profiling/time_width_study.cpp:11-84
+//   exec_cpu_time_width (= exec_time_width) cpu/profiling/time_width_study.cpp:11-84
 // (or `bsj_cli <name> args...`).  Positional arguments, defaults and printed lines are the
 // reference's.  The ICH/PMS drivers run the reference's CPU algorithms as the engine's
 // ICH/PMS modes, on the GPU, with identical makespans for identical rand() seeds.
@@ -413,7 +413,7 @@ int main(int argc, char** argv)
         if (argc < 2) {
             std::fprintf(stderr,
                          "usage: bsj_cli <exec_gpu_v1|exec_gpu_v2|exec_gpu_v1_bench|exec_gpu_v2_bench|"
-                         "BS-ICH|BS-PMS|BS-PMS-bench|exec_time_width> [args]\n");
+                         "BS-ICH|BS-PMS|BS-PMS-bench|exec_cpu_time_width> [args]\n");
             return 2;
         }
         tool = argv[1];
@@ -428,7 +428,7 @@ int main(int argc, char** argv)
     if (tool == "BS-ICH") return main_ich(o);
     if (tool == "BS-PMS") return main_pms(o);
     if (tool == "BS-PMS-bench") return main_suite(o, BSJ_MODE_PMS, 100, "All instances finished.");
-    if (tool == "exec_time_width") return main_time_width(o);
+    if (tool == "exec_cpu_time_width" || tool == "exec_time_width") return main_time_width(o);
     std::fprintf(stderr, "bsj_cli: unknown driver name '%s'\n", tool.c_str());
     return 2;
 }

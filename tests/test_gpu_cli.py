@@ -105,7 +105,7 @@ def test_suites_resolve_ids_and_print_rows(tmp_path, name, mode, iters):
 def test_time_width_sweep(tmp_path):
     mc, du = synthetic_instance(6, 3, 7)
     write_instance(str(tmp_path / "la10.txt"), mc, du)
-    out = _cli("exec_time_width", "--ids", "10", "--iters", 1, "--seed", 2, cwd=str(tmp_path))
+    out = _cli("exec_cpu_time_width", "--ids", "10", "--iters", 1, "--seed", 2, cwd=str(tmp_path))
     widths = [int(line.split()[0]) for line in out.splitlines() if line.split() and line.split()[0].isdigit()]
     assert widths == [100, 200, 400, 800, 1600, 3200, 6400, 12800, 25600]
     assert "width above the engine's limit" in out
