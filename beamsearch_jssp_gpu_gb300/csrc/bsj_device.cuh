@@ -69,6 +69,9 @@ struct SegDesc {
     int64_t hist_off;     // u32 index: per-level (parent << 8 | job) history
     int64_t aux_off;      // byte offset: ICH/PMS per-parent child table
     int64_t seq_off;      // i32 index: result sequence
+    int64_t pos_off[2];   // byte offsets (gpu-v2/clean): per state and branch b, the ready-list
+                          // position of branch b's op (0xFF past the last branch); ping-pong by
+                          // level parity
 };
 
 struct SegState {

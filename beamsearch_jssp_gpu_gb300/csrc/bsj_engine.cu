@@ -218,7 +218,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
 
     // per-beam layout
     size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0, off_kcnt = 0,
-           off_aux = 0, off_seq = 0;
+           off_aux = 0, off_seq = 0, off_pos = 0;
     int sb_max = 16, aux_max = 16, max_n = 1;
     p->prefix.push_back(0);
     p->cprefix.push_back(0);
@@ -265,6 +265,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         if (!gpu) off_aux += align_up(K * d.auxbytes, 256);
         d.seq_off = (int64_t)off_seq;
         off_seq += align_up(N, 64);
+        d.pos_off[0] = d.pos_off[1] = (int64_t)off_pos;
+        if (d.mode == BSJ_MODE_V2 || d.mode == BSJ_MODE_CLEAN) {
+            d.pos_off[1] = (int64_t)(off_pos + align_up(K * n, 256));
+            off_pos += 2 * align_up(K * n, 256);
+        }
         p->segs.push_back(d);
         p->prefix.push_back(p->prefix.back() + d.K);
         p->cprefix.push_back(p->cprefix.back() + nch);
@@ -329,6 +334,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     const size_t o_hist = take(4 * off_hist);
     const size_t o_aux = take(off_aux);
     const size_t o_seq = take(4 * off_seq);
+    const size_t o_pos = take(off_pos);
+    const size_t o_noise = take(1000 * sizeof(float));
     p->mem_bytes = o;
     p->beam_bytes = off_beam;
     p->slot_bytes = off_slot;
@@ -384,6 +391,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.ops = reinterpret_cast<const uint32_t*>(base + o_ops);
     a.group_best = p->d_group;
     a.seq_pool = reinterpret_cast<int32_t*>(base + o_seq);
+    a.pos_pool = base + o_pos;
+    a.noise = reinterpret_cast<const float*>(base + o_noise);
 
     // uploads (synchronous: the host vectors are pageable)
     cudaStream_t st = ctx->stream;
@@ -394,6 +403,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_cprefix, p->cprefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_ops, ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_noise_table(reinterpret_cast<float*>(base + o_noise), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         if (p->owns_mem) cudaFree(p->mem);

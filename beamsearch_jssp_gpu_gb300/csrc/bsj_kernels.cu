@@ -268,6 +268,16 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
         acc += __popc(vb[q]);
     }
     if (lane == 0) *nv_out = nv;
+    if ((d.mode == MODE_V2 || d.mode == MODE_CLEAN) && t < d.N - 1) {
+        // branch b -> ready position of its op, read by the next level's materialisation
+        uint8_t* row = a.pos_pool + d.pos_off[t & 1] + (int64_t)c * L.n;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const int i = lane + 32 * q;
+            if ((C.bal[q] >> lane) & 1u) row[C.bidx[q]] = (uint8_t)i;
+            if (i >= C.cnt && i < L.n) row[i] = 0xFFu;
+        }
+    }
 #pragma unroll
     for (int w = 0; w < NQ; w++) {
         if (w < d.words) {
@@ -336,7 +346,10 @@ __device__ void expand_compat(uint8_t* sb, const Lay& L, const SegDesc& d, const
 // so the copies of later ranks overlap the work on earlier ones.  NQ = ceil(n/32).
 // ------------------------------------------------------------------------------------
 template <int NQ>
-__global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int s)
+#ifndef BSJ_STEP_MIN_BLOCKS
+#define BSJ_STEP_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kWarpsPerStepCta * 32, BSJ_STEP_MIN_BLOCKS) k_step(StepArgs a, int s)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ float s_noise[1000];
@@ -348,8 +361,7 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int 
     // leave in slot order: ranks ascending, branches ascending
     unsigned long long* kstage = reinterpret_cast<unsigned long long*>(
         smem + (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * a.sb_max);
-    for (int k = threadIdx.x; k < 1000; k += blockDim.x)
-        s_noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
+    for (int k = threadIdx.x; k < 1000; k += blockDim.x) s_noise[k] = __ldg(a.noise + k);
     for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
         const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
         const SegDesc& d = a.segs[seg];
@@ -368,11 +380,15 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int 
         const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
         if (mode == MODE_V1) childbuf = a.beam_pool + d.beam_off[0];
 
-        // selection entries of this warp's ranks (one lane each)
-        uint32_t my_e = 0;
+        // selection entries of this warp's ranks (one lane each) and, for the gpu modes,
+        // the ready-list position of the selected branch's op
+        uint32_t my_e = 0, my_pos = 0xFFu;
         if (lane < kRanksPerWarp && s >= 0) {
             const int r = r0 + lane * kWarpsPerStepCta;
-            if (r < P && mode != MODE_V1) my_e = __ldg(a.sel + d.sel_off + r);
+            if (r < P && mode != MODE_V1) {
+                my_e = __ldg(a.sel + d.sel_off + r);
+                if (!compat) my_pos = __ldg(a.pos_pool + d.pos_off[s & 1] + (my_e & ~kFillerFlag));
+            }
         }
         // start all source copies
 #pragma unroll
@@ -411,23 +427,12 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_step(StepArgs a, int 
                 if (lane == 0) hrow[r] = ((uint32_t)c << 8) | (uint32_t)j;
             } else if (mode != MODE_V1) {
                 const uint32_t slot = e & ~kFillerFlag;
-                const int c = (int)(slot / (uint32_t)L.n), b = (int)(slot % (uint32_t)L.n);
-                ReadyOps<NQ> R;
-                load_ready<NQ>(sb, L, a.ops, d.op_off, lane, R);
-                Cands<NQ> C;
-                pivot_candidates<NQ>(R, d.seed + (uint32_t)s, (uint32_t)c, lane, C);
-                if (b < C.cnt) {
-                    // kernel_materialize_topk (gpu/v2_twophases/solver.cu:193-252)
-                    int ii = -1, j = 0;
-#pragma unroll
-                    for (int qq = 0; qq < NQ; qq++) {
-                        unsigned hit = __ballot_sync(FULL_MASK, ((C.bal[qq] >> lane) & 1u) && C.bidx[qq] == b);
-                        if (hit) {
-                            const int l = __ffs(hit) - 1;
-                            ii = 32 * qq + l;
-                            j = __shfl_sync(FULL_MASK, R.job[qq], l);
-                        }
-                    }
+                const int c = (int)(slot / (uint32_t)L.n);
+                const int ii = (int)__shfl_sync(FULL_MASK, my_pos, i);
+                if (ii != 0xFF) {
+                    // kernel_materialize_topk (gpu/v2_twophases/solver.cu:193-252): the
+                    // parent's expansion recorded where branch b's op sits in its ready list
+                    const int j = RD(sb, L)[ii];
                     apply_child<NQ>(sb, L, a.ops, d.op_off, ii, false, ((uint32_t)c << 8) | (uint32_t)j,
                                     (uint32_t)(s + 1), lane);
                     warp_store(childbuf + (int64_t)r * L.sbytes, sb, L.sbytes, lane);
@@ -1644,6 +1649,20 @@ cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stag
                         cudaStream_t stream)
 {
     k_heap<<<a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes), stream>>>(a, s, chunk, stage_bytes);
+    return cudaGetLastError();
+}
+
+// The 1000 possible noise quotients of the gpu solvers' score, (float)(h % 1000) / 1e9f
+// (gpu/v1/solver.cu:127), with the IEEE round-to-nearest division the reference compiles to.
+__global__ void k_noise_table(float* noise)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < 1000) noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
+}
+
+cudaError_t launch_noise_table(float* noise, cudaStream_t stream)
+{
+    k_noise_table<<<4, 256, 0, stream>>>(noise);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,8 @@ struct StepArgs {
     const uint32_t* ops;          // (duration << 8) | machine per op, per instance
     int32_t* group_best;
     int32_t* seq_pool;
+    uint8_t* pos_pool;            // branch -> ready position tables (SegDesc::pos_off)
+    const float* noise;           // [1000]: (float)k / 1e9f, IEEE round-to-nearest
 };
 
 // Grid / shared-memory sizing helpers.
@@ -52,6 +54,8 @@ cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t st
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream);
 cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
                         cudaStream_t stream);
+// Fills noise[0..1000) with (float)k / 1e9f (once per plan; k_step copies it per CTA).
+cudaError_t launch_noise_table(float* noise, cudaStream_t stream);
 cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream);
 cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n);
 // Raise (never lower) the dynamic shared-memory limits of k_select and k_step to what

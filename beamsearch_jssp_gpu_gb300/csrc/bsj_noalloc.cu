@@ -140,10 +140,14 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     const size_t o_mask = take(K * d.words * 4);
     const size_t o_hist = take(N * K * 4);
     const size_t o_seq = take(N * 4);
+    const size_t o_pos = take(2 * align_up(K * n, 256));
+    const size_t o_noise = take(1000 * sizeof(float));
     if (o > kScratchBytes) return BSJ_ERR_LIMIT;  // beam_width x n*m too large for the scratch
     d.beam_off[0] = 0;
     d.beam_off[1] = (int64_t)align_up(K * d.sbytes, 256);
     d.key_off = d.sel_off = d.mask_off = d.hist_off = d.aux_off = d.seq_off = d.slot_off = 0;
+    d.pos_off[0] = 0;
+    d.pos_off[1] = (int64_t)align_up(K * n, 256);
 
     void* base_v = nullptr;
     if (scratch_address(&base_v) != cudaSuccess) return BSJ_ERR_CUDA;
@@ -186,6 +190,8 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     a.ops = reinterpret_cast<const uint32_t*>(base + o_ops);
     a.group_best = reinterpret_cast<int32_t*>(base + o_group);
     a.seq_pool = reinterpret_cast<int32_t*>(base + o_seq);
+    a.pos_pool = base + o_pos;
+    a.noise = reinterpret_cast<const float*>(base + o_noise);
 
     int sort_cap = 1;
     while (sort_cap < beam_width) sort_cap <<= 1;
@@ -207,6 +213,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     k_noalloc_pack<<<1, 256, 0, s>>>(d_machine, d_duration, d.N, m, reinterpret_cast<uint32_t*>(base + o_ops),
                                      reinterpret_cast<SegState*>(base + o_state));
     if (cudaGetLastError() != cudaSuccess) return BSJ_ERR_CUDA;
+    if (launch_noise_table(reinterpret_cast<float*>(base + o_noise), s) != cudaSuccess) return BSJ_ERR_CUDA;
     if (launch_step(a, -1, grid, nq_mask, s) != cudaSuccess) return BSJ_ERR_CUDA;
     for (int lv = 0; lv < d.N; lv++) {
         if (launch_select(a, lv, sort_cap, s) != cudaSuccess) return BSJ_ERR_CUDA;
