@@ -25,7 +25,10 @@
 
 using namespace bsj;
 
-constexpr int kMaxBranches = 8;
+#ifndef BSJ_MAX_BRANCHES
+#define BSJ_MAX_BRANCHES 8
+#endif
+constexpr int kMaxBranches = BSJ_MAX_BRANCHES;  // beam groups run as concurrent graph branches
 
 struct bsj_context {
     int device = 0;

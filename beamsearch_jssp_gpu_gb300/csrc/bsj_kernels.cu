@@ -227,7 +227,9 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
 
     unsigned long long key[NQ];
     unsigned vb[NQ];
-    uint32_t wacc[4] = {0u, 0u, 0u, 0u};
+    // scored-branch mask words of this parent (b < n <= 128), kept in registers: a
+    // dynamically indexed array would live in local memory
+    uint32_t wacc0 = 0u, wacc1 = 0u, wacc2 = 0u, wacc3 = 0u;
 #pragma unroll
     for (int q = 0; q < NQ; q++) {
         bool valid = false;
@@ -245,7 +247,12 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
                 const float sc = __fadd_rn(base, s_noise[noise_hash(seed_t, (uint32_t)c, (uint32_t)b) % 1000u]);
                 const uint32_t slot = (uint32_t)(c * L.n + b);
                 key[q] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
-                wacc[b >> 5] |= 1u << (b & 31);
+                const uint32_t bit = 1u << (b & 31);
+                const int w = b >> 5;
+                wacc0 |= (w == 0) ? bit : 0u;
+                wacc1 |= (w == 1) ? bit : 0u;
+                wacc2 |= (w == 2) ? bit : 0u;
+                wacc3 |= (w == 3) ? bit : 0u;
                 if (last && ns1 == d.N) {
                     atomicMin(&st.best, ((unsigned long long)(uint32_t)cm << 32) |
                                             ((unsigned long long)slot << 8) | (uint32_t)R.job[q]);
@@ -281,7 +288,8 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
 #pragma unroll
     for (int w = 0; w < NQ; w++) {
         if (w < d.words) {
-            uint32_t word = __reduce_or_sync(FULL_MASK, wacc[w]);
+            const uint32_t mine = w == 0 ? wacc0 : (w == 1 ? wacc1 : (w == 2 ? wacc2 : wacc3));
+            uint32_t word = __reduce_or_sync(FULL_MASK, mine);
             if (lane == 0) a.masks[d.mask_off + (int64_t)c * d.words + w] = word;
         }
     }
@@ -349,7 +357,8 @@ template <int NQ>
 #ifndef BSJ_STEP_MIN_BLOCKS
 #define BSJ_STEP_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(kWarpsPerStepCta * 32, BSJ_STEP_MIN_BLOCKS) k_step(StepArgs a, int s)
+// four resident CTAs per SM (64 registers); the n > 64 instance needs more registers
+__global__ void __launch_bounds__(kWarpsPerStepCta * 32, NQ == 4 ? 3 : BSJ_STEP_MIN_BLOCKS) k_step(StepArgs a, int s)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ float s_noise[1000];
