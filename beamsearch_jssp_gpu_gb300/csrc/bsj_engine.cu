@@ -15,6 +15,7 @@
 // 256-386).  The whole sequence is captured once into a CUDA graph and replayed.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -425,9 +426,15 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     p->step_grid = std::max(1, std::min(p->total_chunks, 65535));
     int want = (p->total_ranks + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
     p->gather_grid = std::max(1, std::min(want, ctx->sm_count * 8));
-    // beam groups, balanced by work (K * levels)
+    // beam groups, balanced by work (K * levels); BSJ_MAX_BEAM_GROUPS in the environment
+    // lowers the number of concurrent groups (1 = all beams in lockstep, for measurements)
     {
-        const int G = std::min(nbeams, kMaxBranches);
+        int gmax = kMaxBranches;
+        if (const char* env = std::getenv("BSJ_MAX_BEAM_GROUPS")) {
+            const int v = std::atoi(env);
+            if (v >= 1 && v < gmax) gmax = v;
+        }
+        const int G = std::min(nbeams, gmax);
         double total = 0;
         for (int b = 0; b < nbeams; b++) total += (double)p->segs[b].K * p->segs[b].N;
         int lo = 0;
