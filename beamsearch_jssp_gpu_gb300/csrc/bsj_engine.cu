@@ -1,7 +1,7 @@
 // bsj_engine.cu -- host engine and the C ABI (include/bsj.h).
 //
 // A plan is a set of beams (independent seeds and/or instances of uneven size, any mix
-// of modes) laid out in one device arena.  Running a plan enqueues every search level:
+// of modes) laid out in one device allocation.  Running a plan enqueues every search level:
 //
 //   k_step(-1)                                   roots + level-0 expansion
 //   for s = 0 .. maxN-1:
@@ -38,9 +38,6 @@ struct bsj_context {
     std::string err;
     int sm_count = 0;
     int max_smem_optin = 0;
-    // grow-only device arena reused by bsj_solve / bsj_solve_batch
-    void* arena = nullptr;
-    size_t arena_bytes = 0;
     // plans of recent batch shapes (most recent last), reused with new data
     std::vector<std::pair<std::string, bsj_plan*>> cache;
     uint64_t hits = 0;
@@ -77,7 +74,6 @@ struct bsj_plan {
     // device
     void* mem = nullptr;
     size_t mem_bytes = 0;
-    bool owns_mem = true;
     SegDesc* d_segs = nullptr;
     SegState* d_state = nullptr;
     SegState* d_state_init = nullptr;
@@ -162,25 +158,12 @@ bsj_status validate_instance(bsj_context* ctx, const bsj_instance& in)
     return BSJ_OK;
 }
 
-bsj_status ensure_arena(bsj_context* ctx, size_t bytes)
-{
-    if (ctx->arena_bytes >= bytes) return BSJ_OK;
-    if (ctx->arena) cudaFree(ctx->arena);
-    ctx->arena = nullptr;
-    ctx->arena_bytes = 0;
-    size_t want = std::max(bytes, (size_t)1 << 20);
-    cudaError_t e = cudaMalloc(&ctx->arena, want);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(arena)");
-    ctx->arena_bytes = want;
-    return BSJ_OK;
-}
-
 std::string shape_key(int ninst, const bsj_instance* insts, int nbeams, const bsj_beam* beams);
 
 // With `bytes_only` non-null, computes the plan's device footprint into it and allocates
 // nothing (*out is left untouched).
 bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, int nbeams,
-                      const bsj_beam* beams, bool use_arena, bsj_plan** out, size_t* bytes_only = nullptr)
+                      const bsj_beam* beams, bsj_plan** out, size_t* bytes_only = nullptr)
 {
     if (!ctx || (!out && !bytes_only) || ninst < 1 || nbeams < 1 || !insts || !beams)
         return fail(ctx, BSJ_ERR_INVALID, "plan: null argument or empty batch");
@@ -318,7 +301,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return fail(ctx, BSJ_ERR_LIMIT, "beam too wide for the shared-memory select");
     }
 
-    // device arena layout
+    // device memory layout (one allocation)
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return at; };
     const size_t o_segs = take(sizeof(SegDesc) * nbeams);
@@ -349,15 +332,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return BSJ_OK;
     }
 
-    if (use_arena) {
-        bsj_status s = ensure_arena(ctx, o);
-        if (s != BSJ_OK) { delete p; return s; }
-        p->mem = ctx->arena;
-        p->owns_mem = false;
-    } else {
+    {
         cudaError_t e = cudaMalloc(&p->mem, o);
         if (e != cudaSuccess) { delete p; return cuda_fail(ctx, e, "cudaMalloc(plan)"); }
-        p->owns_mem = true;
     }
     uint8_t* base = static_cast<uint8_t*>(p->mem);
     p->d_segs = reinterpret_cast<SegDesc*>(base + o_segs);
@@ -410,14 +387,14 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     if (e == cudaSuccess) e = launch_noise_table(reinterpret_cast<float*>(base + o_noise), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
-        if (p->owns_mem) cudaFree(p->mem);
+        cudaFree(p->mem);
         delete p;
         return cuda_fail(ctx, e, "plan upload");
     }
 
     e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16), sb_max, max_n);
     if (e != cudaSuccess) {
-        if (p->owns_mem) cudaFree(p->mem);
+        cudaFree(p->mem);
         delete p;
         return cuda_fail(ctx, e, "configure kernels");
     }
@@ -732,7 +709,6 @@ void bsj_destroy(bsj_context* ctx)
     cudaSetDevice(ctx->device);
     for (auto& kv : ctx->cache) bsj_plan_destroy(kv.second);
     ctx->cache.clear();
-    if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     for (cudaStream_t b : ctx->branch)
         if (b) cudaStreamDestroy(b);
@@ -746,7 +722,7 @@ bsj_status bsj_plan_create(bsj_context* ctx, int num_instances, const bsj_instan
 {
     if (!ctx) return BSJ_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    return plan_build(ctx, num_instances, instances, num_beams, beams, false, out);
+    return plan_build(ctx, num_instances, instances, num_beams, beams, out);
 }
 
 bsj_status bsj_plan_estimate(bsj_context* ctx, int num_instances, const bsj_instance* instances,
@@ -754,7 +730,7 @@ bsj_status bsj_plan_estimate(bsj_context* ctx, int num_instances, const bsj_inst
 {
     if (!ctx || !device_bytes) return BSJ_ERR_INVALID;
     size_t bytes = 0;
-    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, false, nullptr, &bytes);
+    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, nullptr, &bytes);
     if (s == BSJ_OK) *device_bytes = (int64_t)bytes;
     return s;
 }
@@ -841,7 +817,7 @@ void bsj_plan_destroy(bsj_plan* p)
         cudaEventDestroy(ev.second.first);
         cudaEventDestroy(ev.second.second);
     }
-    if (p->owns_mem && p->mem) cudaFree(p->mem);
+    if (p->mem) cudaFree(p->mem);
     delete p;
 }
 
@@ -945,7 +921,7 @@ bsj_status solve_batch_impl(bsj_context* ctx, int num_instances, const bsj_insta
         return s;
     }
     bsj_plan* p = nullptr;
-    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, false, &p);
+    bsj_status s = plan_build(ctx, num_instances, instances, num_beams, beams, &p);
     if (s == BSJ_OK && rand_in) {
         s = plan_put_rand(p, rand_in);
         if (s != BSJ_OK) bsj_plan_destroy(p);

@@ -1034,24 +1034,6 @@ __device__ void lsd_sort_emit(unsigned long long* A, unsigned long long* B, int 
     for (int i = threadIdx.x; i < R; i += blockDim.x) sel[i] = (uint32_t)(out[i] & 0xFFFFFFFFull);
 }
 
-// Any element count up to 8 per thread.
-__device__ unsigned long long* lsd_sort_any(unsigned long long* A, unsigned long long* B, int count,
-                                            const SelSmem& S)
-{
-    const int E = (count + (int)blockDim.x - 1) / (int)blockDim.x;
-    switch (E) {
-    case 0:
-    case 1: return lsd_sort<1>(A, B, count, S);
-    case 2: return lsd_sort<2>(A, B, count, S);
-    case 3: return lsd_sort<3>(A, B, count, S);
-    case 4: return lsd_sort<4>(A, B, count, S);
-    case 5: return lsd_sort<5>(A, B, count, S);
-    case 6: return lsd_sort<6>(A, B, count, S);
-    case 7: return lsd_sort<7>(A, B, count, S);
-    default: return lsd_sort<8>(A, B, count, S);
-    }
-}
-
 // in-thread compare-exchange stage of distance J (< E) on the blocked layout i = t*E + e
 template <int E, int J>
 __device__ __forceinline__ void bitonic_in_thread(unsigned long long (&x)[E], int t, int k)

@@ -182,6 +182,26 @@ def _traffic(kernel: str):
     return None
 
 
+def replica_seeds(rank: int):
+    """Search seeds of one replica's beams: rank r runs seeds 8r .. 8r+7, so the N replicas
+    together run N*8 distinct seeds (the reference's MPI ranks, gpu/v1/main.cu:56-60)."""
+    return [BEAMS * rank + b for b in range(BEAMS)]
+
+
+def aggregate_replicas(t_local: float, units_local: float, dist, device: str):
+    """Whole-job figures over the replicas: the slowest rank's time and the units of all
+    ranks (value = units / time).  Without a process group the local figures."""
+    if not dist:
+        return float(t_local), float(units_local)
+    import torch
+
+    tt = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    uu = torch.tensor([float(units_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(uu)
+    return float(tt.item()), float(uu.item())
+
+
 def gpu_arm(args) -> int:
     import numpy as np
     import torch
@@ -209,7 +229,7 @@ def gpu_arm(args) -> int:
 
     mc, du = synthetic_instance(N_JOBS, N_MACH, INSTANCE_SEED)
     ctx = Context(local)
-    beams = [BeamSpec(MODE, K, 500000, BEAMS * rank + b, 0, 0) for b in range(BEAMS)]
+    beams = [BeamSpec(MODE, K, 500000, sd, 0, 0) for sd in replica_seeds(rank)]
     plan = ctx.plan([(mc, du)], beams)
     stream = torch.cuda.Stream()            # explicit stream: a handle of 0 would select the context's own
     sh = stream.cuda_stream
@@ -251,16 +271,7 @@ def gpu_arm(args) -> int:
         kms = plan.kernel_ms()
     expanded = sum(r["expanded"] for r in res)
     launches_per_step = plan.launches
-    t_step = sum(times) / len(times)
-    if dist:
-        tt = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
-        ex = torch.tensor([expanded], dtype=torch.float64, device="cuda")
-        dist.all_reduce(ex)
-        expanded_all = float(ex.item())
-    else:
-        expanded_all = float(expanded)
+    t_step, expanded_all = aggregate_replicas(sum(times) / len(times), expanded, dist, "cuda")
     value = expanded_all / (t_step / 1000.0)
 
     # e2e: the C ABI from host buffers (instance upload + all levels + results/schedules back)
@@ -275,11 +286,7 @@ def gpu_arm(args) -> int:
             if k >= args.warmup:
                 e2e_times.append(t1 - t0)
             assert sum(r["expanded"] for r in out) == expanded
-    e2e_t = sum(e2e_times) / len(e2e_times)
-    if dist:
-        tt = torch.tensor([e2e_t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t, _ = aggregate_replicas(sum(e2e_times) / len(e2e_times), 0, dist, "cuda")
     h2d = mc.nbytes + du.nbytes + 24 * BEAMS
     d2h = BEAMS * (N_JOBS * N_MACH * 4 + 48)
 

@@ -202,3 +202,18 @@ def test_cli_names_and_argument_errors(lib, tmp_path):
     assert r.returncode == 1 and "unknown option" in r.stderr
     r = _cli("exec_gpu_v2", str(tmp_path / "i.txt"), "--ranks", "0")
     assert r.returncode == 1
+
+
+def test_without_a_device_contexts_and_servers_fail_cleanly(lib):
+    """No call exits or hangs when no GPU is usable: status codes come back."""
+    count = ctypes.c_int32(-1)
+    st = lib.bsj_device_count(ctypes.byref(count))
+    if st == nat.BSJ_OK and count.value > 0:
+        pytest.skip("a CUDA device is present")
+    assert count.value == 0
+    h = ctypes.c_void_p()
+    assert lib.bsj_create(ctypes.byref(h), 0) != nat.BSJ_OK
+    from beamsearch_jssp_gpu_gb300 import BsjError, Server
+
+    with pytest.raises(BsjError):
+        Server(0)
