@@ -602,6 +602,17 @@ struct KeySrc {
         }
         return base[(size_t)lo * cap + (i - cpref[lo])];
     }
+    // fn(key) on every key, warp per chunk (order not preserved)
+    template <typename Fn>
+    __device__ __forceinline__ void each_key(Fn fn) const
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int c = warp; c < nch; c += nw) {
+            const int c0 = cpref[c], nc = cpref[c + 1] - c0;
+            const unsigned long long* src = base + (size_t)c * cap;
+            for (int j = lane; j < nc; j += 32) fn(src[j]);
+        }
+    }
     // keys i0 .. i0+KPT-1 (~0 past V): one search, then walk the chunks
     template <int KPT>
     __device__ __forceinline__ void load_run(int i0, int V, unsigned long long (&out)[KPT]) const
@@ -665,15 +676,16 @@ __device__ void stage_keys(const KeySrc& ks, unsigned long long* stg)
 
 // 2a. bucket threshold: returns the number of keys in buckets <= T; misc[2] = T,
 // misc[4] = shift, misc[1] = smin.
-template <typename Get>
-__device__ int bucket_threshold(Get get, int V, int R, const SelSmem& S)
+// `each(fn)` calls fn on every key this thread is responsible for.
+template <typename ForEach>
+__device__ int bucket_threshold_each(ForEach each, int R, const SelSmem& S)
 {
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31;
     uint32_t* cnt = S.hist;
     int* misc = S.misc;
     int* wsum = reinterpret_cast<int*>(S.red);
     uint32_t mn = 0xFFFFFFFFu, mx = 0u;
-    for (int i = tid; i < V; i += nthr) { uint32_t sb = (uint32_t)(get(i) >> 32); mn = min(mn, sb); mx = max(mx, sb); }
+    each([&](unsigned long long k) { const uint32_t sb = (uint32_t)(k >> 32); mn = min(mn, sb); mx = max(mx, sb); });
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
@@ -690,7 +702,7 @@ __device__ int bucket_threshold(Get get, int V, int R, const SelSmem& S)
     const uint32_t smin = (uint32_t)misc[1], range = (uint32_t)misc[0] - smin;
     const int nbits = range ? 32 - __clz(range) : 0;
     const int shift = nbits > 12 ? nbits - 12 : 0;
-    for (int i = tid; i < V; i += nthr) atomicAdd(&cnt[(((uint32_t)(get(i) >> 32)) - smin) >> shift], 1u);
+    each([&](unsigned long long k) { atomicAdd(&cnt[(((uint32_t)(k >> 32)) - smin) >> shift], 1u); });
     __syncthreads();
     constexpr int BPT = kNB / kSelectThreads;
     uint32_t c4[BPT];
@@ -707,6 +719,13 @@ __device__ int bucket_threshold(Get get, int V, int R, const SelSmem& S)
     if (tid == 0) misc[4] = shift;
     __syncthreads();
     return misc[3];
+}
+
+template <typename Get>
+__device__ int bucket_threshold(Get get, int V, int R, const SelSmem& S)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    return bucket_threshold_each([&](auto fn) { for (int i = tid; i < V; i += nthr) fn(get(i)); }, R, S);
 }
 
 // 2b. radix threshold: exact R-th key; returns (pmask, prefix) with keep = (k & pmask) <= prefix.
@@ -861,15 +880,42 @@ constexpr int kDenseBmOff = kLsdMax + kNB / 4;     // u32[kDenseWords] bitmap, t
 constexpr int kDenseWords = 4096;
 static_assert(kDenseBmOff + kDenseWords <= kStageKeys, "dense-rank tables exceed the staging area");
 
-__device__ bool dense_rank_keys(unsigned long long* A, int count, int T, int shift, uint32_t smin,
-                                const SelSmem& S)
+// Dense-rank tables over the occupied buckets <= T: a bitmap of the distinct scores
+// (2^shift bits per occupied bucket) and the popcount prefix of its words.
+struct DenseTables {
+    uint16_t* occ;   // [kNB] occupied-bucket index
+    uint32_t* bm;    // [kDenseWords] bitmap
+    uint32_t* wp;    // [kDenseWords] exclusive popcount prefix of bm
+    int W;           // bitmap words per occupied bucket
+    int shift;
+    uint32_t smin, omask;
+    __device__ __forceinline__ int word_of(uint32_t score_bits, uint32_t& bit) const
+    {
+        const uint32_t dd = score_bits - smin;
+        const uint32_t off = dd & omask;
+        bit = off & 31u;
+        return (int)occ[dd >> shift] * W + (int)(off >> 5);
+    }
+    // rank of a score among the distinct scores marked in the bitmap
+    __device__ __forceinline__ uint32_t rank_of(uint32_t score_bits) const
+    {
+        uint32_t bit;
+        const int w = word_of(score_bits, bit);
+        return wp[w] + (uint32_t)__popc(bm[w] & ((1u << bit) - 1u));
+    }
+};
+
+// Builds the tables for the keys `each` visits whose bucket is <= T (`each(fn)` calls fn on
+// every key this thread is responsible for).  Returns the number of distinct scores, or -1
+// (tables unusable) when the bitmap would exceed kDenseWords words.
+template <typename ForEach>
+__device__ int dense_build(ForEach each, int T, int shift, uint32_t smin, const SelSmem& S, DenseTables& D)
 {
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int W = shift > 5 ? 1 << (shift - 5) : 1;   // bitmap words per occupied bucket
-    const uint32_t omask = (1u << shift) - 1u;
-    uint16_t* occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
-    uint32_t* bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
-    uint32_t* wp = bm + kDenseWords;
+    D.W = shift > 5 ? 1 << (shift - 5) : 1;
+    D.shift = shift;
+    D.smin = smin;
+    D.omask = (1u << shift) - 1u;
     int* wsum = reinterpret_cast<int*>(S.red);
     constexpr int BPT = kNB / kSelectThreads;
     int f[BPT], sum = 0;
@@ -883,42 +929,57 @@ __device__ bool dense_rank_keys(unsigned long long* A, int count, int T, int shi
     int base = block_exclusive_scan(sum, &O, wsum);
 #pragma unroll
     for (int u = 0; u < BPT; u++) {
-        occ[tid * BPT + u] = (uint16_t)base;
+        D.occ[tid * BPT + u] = (uint16_t)base;
         base += f[u];
     }
-    const int nw = O * W;
-    if (nw > kDenseWords) return false;   // O is the same in every thread
-    for (int w = tid; w < nw; w += nthr) bm[w] = 0u;
+    const int nw = O * D.W;
+    if (nw > kDenseWords) return -1;   // O is the same in every thread
+    for (int w = tid; w < nw; w += nthr) D.bm[w] = 0u;
     __syncthreads();
-    for (int i = tid; i < count; i += nthr) {
-        const uint32_t d = (uint32_t)(A[i] >> 32) - smin;
-        const uint32_t off = d & omask;
-        atomicOr(&bm[(int)occ[d >> shift] * W + (int)(off >> 5)], 1u << (off & 31u));
-    }
+    const uint32_t lim = ((uint32_t)T + 1u) << shift;
+    each([&](unsigned long long k) {
+        const uint32_t sb = (uint32_t)(k >> 32);
+        if (sb - smin < lim) {
+            uint32_t bit;
+            const int w = D.word_of(sb, bit);
+            atomicOr(&D.bm[w], 1u << bit);
+        }
+    });
     __syncthreads();
     const int per = (nw + nthr - 1) / nthr;
     int c = 0;
     for (int k = 0; k < per; k++) {
         const int w = tid * per + k;
-        if (w < nw) c += __popc(bm[w]);
+        if (w < nw) c += __popc(D.bm[w]);
     }
-    int D;
-    int pre = block_exclusive_scan(c, &D, wsum);
+    int Dn;
+    int pre = block_exclusive_scan(c, &Dn, wsum);
     for (int k = 0; k < per; k++) {
         const int w = tid * per + k;
         if (w < nw) {
-            wp[w] = (uint32_t)pre;
-            pre += __popc(bm[w]);
+            D.wp[w] = (uint32_t)pre;
+            pre += __popc(D.bm[w]);
         }
     }
     __syncthreads();
+    return Dn;
+}
+
+__device__ bool dense_rank_keys(unsigned long long* A, int count, int T, int shift, uint32_t smin,
+                                const SelSmem& S)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    DenseTables D;
+    D.occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
+    D.bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
+    D.wp = D.bm + kDenseWords;
+    auto each = [&](auto fn) {
+        for (int i = tid; i < count; i += nthr) fn(A[i]);
+    };
+    if (dense_build(each, T, shift, smin, S, D) < 0) return false;
     for (int i = tid; i < count; i += nthr) {
         const unsigned long long k = A[i];
-        const uint32_t d = (uint32_t)(k >> 32) - smin;
-        const uint32_t off = d & omask;
-        const int w = (int)occ[d >> shift] * W + (int)(off >> 5);
-        const uint32_t rank = wp[w] + (uint32_t)__popc(bm[w] & ((1u << (off & 31u)) - 1u));
-        A[i] = ((unsigned long long)rank << 32) | (k & 0xFFFFFFFFull);
+        A[i] = ((unsigned long long)D.rank_of((uint32_t)(k >> 32)) << 32) | (k & 0xFFFFFFFFull);
     }
     __syncthreads();
     return true;
@@ -1159,6 +1220,187 @@ __device__ void select_fillers(const SegDesc& d, const StepArgs& a, int P, int R
     }
 }
 
+// ---- large levels: more candidate keys than the staging area holds (V > kStageKeys) or
+// more survivors than the 64-bit radix buffer (K > kLsdMax).  The keys stay in their chunk
+// regions in global memory (L2-resident); survivors are compacted as 32-bit words
+// (dense rank << 21 | slot) into the two 96 KB halves of the A/stg area, and sorted by the
+// rank bits with a stable 8-bit radix pass that needs no per-element registers. ----
+constexpr int kBigCap = kLsdMax + kStageKeys;  // u32 survivors per half of the A/stg area
+constexpr int kSlotBits = 21;                                         // slot < K * n <= 2^21
+constexpr int kBigMaxDistinct = 1 << (32 - kSlotBits);                // ranks in the top 11 bits
+static_assert(2 * kBigCap * 4 == (kLsdMax + kStageKeys) * 8, "two kBigCap u32 halves fill the A/stg area");
+static_assert(kNB / 2 + 2 * kDenseWords <= kBigCap, "dense tables must fit the second half");
+static_assert((long long)kMaxBeam * kMaxJobs <= (1LL << kSlotBits), "slots must fit 21 bits");
+
+// Stable compaction of the keys of buckets <= T (score bits - smin < lim), in slot order,
+// each written as (dense rank << kSlotBits) | slot.  Warps own contiguous runs of chunks:
+// one counting sweep, a scan of the warp totals, one writing sweep.
+__device__ int compact_ranked(const KeySrc& ks, uint32_t lim, uint32_t smin, const DenseTables& D, uint32_t* out,
+                              int cap, const SelSmem& S)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int* wtot = S.misc + 16;   // [32]
+    const int cpw = (ks.nch + nwarps - 1) / nwarps;
+    const int c_lo = min(ks.nch, warp * cpw), c_hi = min(ks.nch, c_lo + cpw);
+    int c = 0;
+    for (int ch = c_lo; ch < c_hi; ch++) {
+        const int nc = ks.cpref[ch + 1] - ks.cpref[ch];
+        const unsigned long long* src = ks.base + (size_t)ch * ks.cap;
+        for (int j0 = 0; j0 < nc; j0 += 32) {
+            const int j = j0 + lane;
+            const bool f = j < nc && ((uint32_t)(src[j] >> 32) - smin) < lim;
+            c += __popc(__ballot_sync(FULL_MASK, f));
+        }
+    }
+    if (lane == 0) wtot[warp] = c;
+    __syncthreads();
+    if (warp == 0) {
+        const int v = lane < nwarps ? wtot[lane] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < nwarps) wtot[lane] = x - v;
+        if (lane == 31) S.misc[60] = x;
+    }
+    __syncthreads();
+    int pos = wtot[warp];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int ch = c_lo; ch < c_hi; ch++) {
+        const int nc = ks.cpref[ch + 1] - ks.cpref[ch];
+        const unsigned long long* src = ks.base + (size_t)ch * ks.cap;
+        for (int j0 = 0; j0 < nc; j0 += 32) {
+            const int j = j0 + lane;
+            unsigned long long k = 0;
+            bool f = false;
+            if (j < nc) {
+                k = src[j];
+                f = ((uint32_t)(k >> 32) - smin) < lim;
+            }
+            const unsigned b = __ballot_sync(FULL_MASK, f);
+            const int at = pos + __popc(b & lt);
+            if (f && at < cap) out[at] = (D.rank_of((uint32_t)(k >> 32)) << kSlotBits) | (uint32_t)(k & 0xFFFFFFFFull);
+            pos += __popc(b);
+        }
+    }
+    const int total = S.misc[60];
+    __syncthreads();
+    return total;
+}
+
+// One stable counting pass of src[0..count) into dst by the 8-bit digit at bit `sh`.
+// Warps own contiguous element runs; a digit's rank inside a 32-element tile comes from the
+// peers' bit ballots, across tiles and warps from per-warp 16-bit counters.  The tiles are
+// walked twice (count, then scatter) so no element state is held across the prefix.
+__device__ void radix_pass32(const uint32_t* src, uint32_t* dst, int count, int sh, const SelSmem& S)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    uint16_t* wh = reinterpret_cast<uint16_t*>(S.hist);   // [32][256]
+    int* dtot = reinterpret_cast<int*>(S.tot);           // [256]
+    const unsigned lt = (1u << lane) - 1u;
+    const int per = ((count + nwarps - 1) / nwarps + 31) & ~31;
+    const int lo = min(count, warp * per), hi = min(count, lo + per);
+    for (int i = tid; i < 32 * 256 / 2; i += blockDim.x) S.hist[i] = 0u;
+    __syncthreads();
+    auto peers = [&](bool valid, int dg) {
+        unsigned grp = __ballot_sync(FULL_MASK, valid);
+#pragma unroll
+        for (int bit = 0; bit < 8; bit++) {
+            const unsigned bb = __ballot_sync(FULL_MASK, (dg >> bit) & 1);
+            grp &= ((dg >> bit) & 1) ? bb : ~bb;
+        }
+        return grp;
+    };
+    for (int i0 = lo; i0 < hi; i0 += 32) {
+        const int i = i0 + lane;
+        const bool valid = i < hi;
+        const int dg = valid ? (int)((src[i] >> sh) & 255u) : 0;
+        const unsigned grp = peers(valid, dg);
+        if (valid && (grp & lt) == 0u) wh[warp * 256 + dg] = (uint16_t)(wh[warp * 256 + dg] + __popc(grp));
+        __syncwarp();
+    }
+    __syncthreads();
+    if (tid < 256) {
+        int run = 0;
+        for (int w = 0; w < nwarps; w++) {
+            const int t = wh[w * 256 + tid];
+            wh[w * 256 + tid] = (uint16_t)run;
+            run += t;
+        }
+        dtot[tid] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int v8[8], sum = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { v8[u] = dtot[lane * 8 + u]; sum += v8[u]; }
+        int xx = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, xx, o);
+            if (lane >= o) xx += y;
+        }
+        int run = xx - sum;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { dtot[lane * 8 + u] = run; run += v8[u]; }
+    }
+    __syncthreads();
+    for (int i0 = lo; i0 < hi; i0 += 32) {
+        const int i = i0 + lane;
+        const bool valid = i < hi;
+        const uint32_t x = valid ? src[i] : 0u;
+        const int dg = (int)((x >> sh) & 255u);
+        const unsigned grp = peers(valid, dg);
+        if (valid) dst[dtot[dg] + (int)wh[warp * 256 + dg] + __popc(grp & lt)] = x;
+        __syncwarp();
+        if (valid && (grp & lt) == 0u) wh[warp * 256 + dg] = (uint16_t)(wh[warp * 256 + dg] + __popc(grp));
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
+// The whole selection of a large level; false (nothing written) when it does not fit
+// these buffers -- then the general path runs.
+__device__ bool select_large(SegState& st, int R, const KeySrc& ks, uint32_t* sel, const SelSmem& S)
+{
+    const int tid = threadIdx.x;
+    auto each = [&](auto fn) { ks.each_key(fn); };
+    const int count0 = bucket_threshold_each(each, R, S);
+    const int T = S.misc[2], shift = S.misc[4];
+    const uint32_t smin = (uint32_t)S.misc[1];
+    __syncthreads();
+    if (count0 > kBigCap) return false;
+    uint32_t* buf1 = reinterpret_cast<uint32_t*>(S.A);
+    uint32_t* buf2 = buf1 + kBigCap;
+    DenseTables D;
+    D.occ = reinterpret_cast<uint16_t*>(buf2);
+    D.bm = buf2 + kNB / 2;
+    D.wp = D.bm + kDenseWords;
+    const int nd = dense_build(each, T, shift, smin, S, D);
+    if (nd < 0 || nd > kBigMaxDistinct) return false;
+    const uint32_t lim = ((uint32_t)T + 1u) << shift;
+    int count = compact_ranked(ks, lim, smin, D, buf1, kBigCap, S);
+    if (count != count0 || count < R) {
+        if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
+        count = min(count, kBigCap);
+    }
+    const int nbits = nd > 1 ? 32 - __clz(nd - 1) : 0;
+    uint32_t* src = buf1;
+    uint32_t* dst = buf2;
+    for (int sh = kSlotBits; sh < kSlotBits + nbits; sh += 8) {
+        radix_pass32(src, dst, count, sh, S);
+        uint32_t* t = src;
+        src = dst;
+        dst = t;
+    }
+    const int RR = R < count ? R : count;
+    for (int i = tid; i < RR; i += blockDim.x) sel[i] = src[i] & ((1u << kSlotBits) - 1u);
+    __syncthreads();
+    return true;
+}
+
 __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int V, const KeySrc& ks,
                            uint8_t* smem)
 {
@@ -1169,9 +1411,11 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
     const int R = V < keff ? V : keff;
     uint32_t* sel = a.sel + d.sel_off;
     const SelSmem S = sel_smem(smem);
-    if (R > 0) {
-        // staged (shared-memory) input when the level fits, else read from global memory
-        const bool staged = (V <= kStageKeys) && (K <= kLsdMax);
+    // staged (shared-memory) input when the level fits; larger levels take select_large
+    const bool staged = (V <= kStageKeys) && (K <= kLsdMax);
+    if (R > 0 && !staged && select_large(st, R, ks, sel, S)) {
+        // done: survivors 0..R-1 written
+    } else if (R > 0) {
         if (staged) stage_keys(ks, S.stg);
         const unsigned long long* stg = S.stg;
         auto get_s = [=](int i) { return stg[i]; };

@@ -91,3 +91,12 @@ def test_invalid_inputs_raise_without_running(ctx):
         ctx.solve_batch([(mc, du)], [BeamSpec("v2", 8, 500000, 0, 3)])
     # the context stays usable
     check(ctx, mc, du, "v2", 8, 0)
+
+
+@pytest.mark.parametrize("mode", ["v1", "v2", "clean"])
+@pytest.mark.parametrize("n,m,K", [(64, 3, 2048), (40, 5, 4096), (30, 6, 8192)])
+def test_large_levels_match_oracle(ctx, mode, n, m, K):
+    """Levels with more candidate keys than the select stages in shared memory (25-35 K per
+    level here), which run the chunk-walking select with 32-bit dense-rank keys."""
+    mc, du = synthetic_instance(n, m, 3)
+    check(ctx, mc, du, mode, K, 5)
