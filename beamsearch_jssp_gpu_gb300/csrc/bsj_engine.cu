@@ -52,6 +52,7 @@ struct bsj_plan {
     int nq_mask = 0;
     int gather_grid = 1;
     int sort_cap = 0, heap_k = 0, heap_chunk = 1, heap_stage = 16;
+    int heap_qn = 0;   // PMS quotient slots per staged parent (largest n; 0 without PMS beams)
     bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
     int step_grid = 1;
     // beam groups: contiguous beam ranges run as independent graph branches, so one
@@ -289,10 +290,13 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     }
     // ICH/PMS staging: two chunks of parents' child tables next to the heap
     if (p->has_compat) {
+        for (int b = 0; b < nbeams; b++)
+            if (p->segs[b].mode == BSJ_MODE_PMS) p->heap_qn = std::max(p->heap_qn, p->segs[b].n);
         size_t budget = (size_t)ctx->max_smem_optin;
-        size_t base = heap_smem_bytes(p->heap_k, 0);
-        if (base + 2 * (size_t)aux_max > budget) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "ICH/PMS beam too wide for shared memory"); }
-        int chunk = (int)std::min<size_t>(32, (budget - base) / (2 * (size_t)aux_max));
+        size_t base = heap_smem_bytes(p->heap_k, 0, 0);
+        const size_t per_parent = 2 * ((size_t)aux_max + sizeof(double) * p->heap_qn);
+        if (base + per_parent > budget) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "ICH/PMS beam too wide for shared memory"); }
+        int chunk = (int)std::min<size_t>(32, (budget - base) / per_parent);
         p->heap_chunk = std::max(1, chunk);
         p->heap_stage = p->heap_chunk * aux_max;
     }
@@ -323,6 +327,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     const size_t o_seq = take(4 * off_seq);
     const size_t o_pos = take(off_pos);
     const size_t o_noise = take(1000 * sizeof(float));
+    const size_t o_dnoise = take(1000 * sizeof(double));
     p->mem_bytes = o;
     p->beam_bytes = off_beam;
     p->slot_bytes = off_slot;
@@ -374,6 +379,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.seq_pool = reinterpret_cast<int32_t*>(base + o_seq);
     a.pos_pool = base + o_pos;
     a.noise = reinterpret_cast<const float*>(base + o_noise);
+    a.dnoise = reinterpret_cast<const double*>(base + o_dnoise);
 
     // uploads (synchronous: the host vectors are pageable)
     cudaStream_t st = ctx->stream;
@@ -384,7 +390,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_cprefix, p->cprefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_ops, ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_noise_table(reinterpret_cast<float*>(base + o_noise), st);
+    if (e == cudaSuccess) e = launch_noise_table(reinterpret_cast<float*>(base + o_noise),
+                                                        reinterpret_cast<double*>(base + o_dnoise), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         cudaFree(p->mem);
@@ -392,7 +399,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return cuda_fail(ctx, e, "plan upload");
     }
 
-    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16), sb_max, max_n);
+    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16),
+                          p->heap_chunk * p->heap_qn * (int)sizeof(double), sb_max, max_n);
     if (e != cudaSuccess) {
         cudaFree(p->mem);
         delete p;
@@ -524,7 +532,7 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
                 if (r != cudaSuccess) return r;
             }
             if (gr.has_compat) {
-                r = timed_g(2, [&] { return launch_heap(ga, lv, p->heap_k, p->heap_chunk, p->heap_stage, gs); });
+                r = timed_g(2, [&] { return launch_heap(ga, lv, p->heap_k, p->heap_chunk, p->heap_stage, p->heap_qn, gs); });
                 if (r != cudaSuccess) return r;
             }
             if (lv < gr.maxN - 1) {

@@ -1532,14 +1532,15 @@ struct HeapSmem {
 };
 
 // hk [K] u64 | hv [K] u32 | ring [64] u32 | misc [16] i32 | (16-aligned) stage [2][stage_bytes]
+// | quotients [2][q_bytes] (PMS: cmax / ns per staged child, as doubles)
 __host__ __device__ __forceinline__ size_t heap_stage_offset(int k)
 {
     return (((size_t)k * 12 + 64 * 4 + 16 * 4) + 15) & ~(size_t)15;
 }
 
-size_t heap_smem_bytes(int max_k, int stage_bytes)
+size_t heap_smem_bytes(int max_k, int stage_bytes, int q_bytes)
 {
-    return heap_stage_offset(max_k) + 2 * (size_t)stage_bytes;
+    return heap_stage_offset(max_k) + 2 * (size_t)stage_bytes + 2 * (size_t)q_bytes;
 }
 
 __device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* hv, int hole, int top,
@@ -1611,7 +1612,8 @@ struct Rng {
     }
 };
 
-__global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes)
+// qn: quotient slots per staged parent (the batch's largest n; 0 when no beam is PMS).
+__global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes, int qn)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const int seg = a.seg_lo + blockIdx.x;
@@ -1632,6 +1634,8 @@ __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int ch
 
     // chunk 0 staged by everyone
     const int nchunks = (P + chunk - 1) / chunk;
+    const bool pms = (d.mode == MODE_PMS) && qn >= n;
+    double* qbuf = reinterpret_cast<double*>(H.stage + 2 * (size_t)stage_bytes);
     auto stage_chunk = [&](int q, int t0, int nt) {
         if (q >= nchunks) return;
         const int c0 = q * chunk;
@@ -1640,7 +1644,25 @@ __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int ch
         uint4* dst = reinterpret_cast<uint4*>(H.stage + (size_t)(q & 1) * stage_bytes);
         for (int u = t0; u < (cnt * ab) >> 4; u += nt) dst[u] = src[u];
     };
+    // BS-PMS score's first quotient, cmax / ns (cpu/v1_pms/solver.cpp:52), for every ready
+    // position of the staged parents, off the serial thread (the pivot is not drawn yet)
+    auto quotients = [&](int q, int t0, int nt) {
+        if (!pms || q >= nchunks) return;
+        const int c0 = q * chunk;
+        const int cnt = (P - c0) < chunk ? (P - c0) : chunk;
+        const uint8_t* sbuf = H.stage + (size_t)(q & 1) * stage_bytes;
+        double* qb = qbuf + (size_t)(q & 1) * chunk * qn;
+        const double ns = (double)(s + 1);
+        for (int u = t0; u < cnt * n; u += nt) {
+            const int cl = u / n, i = u - cl * n;
+            const uint8_t* pa = sbuf + (size_t)cl * ab;
+            if (i < (int)*reinterpret_cast<const uint32_t*>(pa))
+                qb[cl * qn + i] = __ddiv_rn((double)reinterpret_cast<const int32_t*>(pa + 4)[i], ns);
+        }
+    };
     stage_chunk(0, tid, blockDim.x);
+    __syncthreads();
+    quotients(0, tid, blockDim.x);
     __syncthreads();
 
     int size = 0;
@@ -1657,6 +1679,8 @@ __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int ch
     for (int q = 0; q < nchunks; q++) {
         if (tid >= 32) {
             stage_chunk(q + 1, tid - 32, blockDim.x - 32);
+            __syncwarp();
+            quotients(q + 1, tid - 32, blockDim.x - 32);
         } else if (tid == 0) {
             const int c0 = q * chunk;
             const int cend = (P - c0) < chunk ? P : c0 + chunk;
@@ -1683,8 +1707,9 @@ __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int ch
                     for (int i = 0; i < rc; i++) {
                         if (cmv[i] != target) continue;
                         const uint32_t dn = g.next();
-                        const double sc = __dadd_rn(__ddiv_rn((double)cc[i], (double)(s + 1)),
-                                                    __ddiv_rn((double)(dn % 1000u), 1000000.0));
+                        const double qv = pms ? qbuf[(size_t)(q & 1) * chunk * qn + (c - c0) * qn + i]
+                                              : __ddiv_rn((double)cc[i], (double)(s + 1));
+                        const double sc = __dadd_rn(qv, a.dnoise[dn % 1000u]);
                         gen++;
                         if (last && cc[i] < best_cm) {
                             best_cm = cc[i];
@@ -1837,12 +1862,12 @@ static cudaError_t raise_smem(F* fn, size_t bytes)
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int sb_max, int max_n)
+cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int q_bytes, int sb_max, int max_n)
 {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = set_carveout();
     if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e == cudaSuccess) e = raise_smem(k_heap, heap_smem_bytes(max_k, stage_bytes));
+    if (e == cudaSuccess) e = raise_smem(k_heap, heap_smem_bytes(max_k, stage_bytes, q_bytes));
     if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
     if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
     if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
@@ -1880,24 +1905,30 @@ cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes,
+cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes, int qn,
                         cudaStream_t stream)
 {
-    k_heap<<<a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes), stream>>>(a, s, chunk, stage_bytes);
+    const int q_bytes = chunk * qn * (int)sizeof(double);
+    k_heap<<<a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes, q_bytes), stream>>>(
+        a, s, chunk, stage_bytes, qn);
     return cudaGetLastError();
 }
 
 // The 1000 possible noise quotients of the gpu solvers' score, (float)(h % 1000) / 1e9f
 // (gpu/v1/solver.cu:127), with the IEEE round-to-nearest division the reference compiles to.
-__global__ void k_noise_table(float* noise)
+// and of BS-PMS's, (double)(rand() % 1000) / 1000000.0 (cpu/v1_pms/solver.cpp:52-53).
+__global__ void k_noise_table(float* noise, double* dnoise)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < 1000) noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
+    if (k < 1000) {
+        noise[k] = __fdiv_rn(__uint2float_rn((unsigned)k), 1000000000.0f);
+        if (dnoise) dnoise[k] = __ddiv_rn((double)k, 1000000.0);
+    }
 }
 
-cudaError_t launch_noise_table(float* noise, cudaStream_t stream)
+cudaError_t launch_noise_table(float* noise, double* dnoise, cudaStream_t stream)
 {
-    k_noise_table<<<4, 256, 0, stream>>>(noise);
+    k_noise_table<<<4, 256, 0, stream>>>(noise, dnoise);
     return cudaGetLastError();
 }
 

@@ -213,7 +213,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     k_noalloc_pack<<<1, 256, 0, s>>>(d_machine, d_duration, d.N, m, reinterpret_cast<uint32_t*>(base + o_ops),
                                      reinterpret_cast<SegState*>(base + o_state));
     if (cudaGetLastError() != cudaSuccess) return BSJ_ERR_CUDA;
-    if (launch_noise_table(reinterpret_cast<float*>(base + o_noise), s) != cudaSuccess) return BSJ_ERR_CUDA;
+    if (launch_noise_table(reinterpret_cast<float*>(base + o_noise), nullptr, s) != cudaSuccess) return BSJ_ERR_CUDA;
     if (launch_step(a, -1, grid, nq_mask, s) != cudaSuccess) return BSJ_ERR_CUDA;
     for (int lv = 0; lv < d.N; lv++) {
         if (launch_select(a, lv, sort_cap, s) != cudaSuccess) return BSJ_ERR_CUDA;
