@@ -237,7 +237,7 @@ bsj_status bsj_server_get_stats(bsj_server *server, bsj_server_stats *out);
                             found, then the 1-based op sequence
    Asynchronous on `stream` (a cudaStream_t, NULL = default stream).  Returns
    BSJ_ERR_LIMIT when n, m, beam_width exceed the BSJ_MAX_* limits or the beam's working
-   set (about 2*K*(4m+6n+16) + 8*K*n + 4*K*n*m bytes) exceeds the scratch array.  The
+   set (about 2*K*(4m+6n+16) + 10*K*n + 4*K*n*m bytes) exceeds the scratch array.  The
    first call on each device looks up the scratch array's device address: make it before
    any stream capture.  Calls share the scratch array: calls that overlap on one GPU race
    and must be serialised by the caller. */
