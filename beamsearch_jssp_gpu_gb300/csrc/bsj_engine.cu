@@ -71,6 +71,9 @@ struct bsj_plan {
     std::vector<int32_t> cprefix;
     std::vector<int32_t> group_init;
     std::vector<int32_t> seg_group;
+    // segment i holds the caller's beam perm[i]: beams are laid out longest search first so
+    // that the graph branches (contiguous segment ranges) group searches of similar length
+    std::vector<int32_t> perm;
     std::string shape;  // shape_key() of the batch the plan was built for
     // device
     void* mem = nullptr;
@@ -204,13 +207,23 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         p->group_init.assign(next, INT32_MAX);
     }
 
+    // segment order: levels (n*m) descending, then the caller's order
+    p->perm.resize(nbeams);
+    for (int b = 0; b < nbeams; b++) p->perm[b] = b;
+    auto levels_of = [&](int b) {
+        const int i = beams[b].instance;
+        return (i >= 0 && i < ninst) ? insts[i].n * insts[i].m : 0;
+    };
+    std::stable_sort(p->perm.begin(), p->perm.end(), [&](int x, int y) { return levels_of(x) > levels_of(y); });
+
     // per-beam layout
     size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0, off_kcnt = 0,
            off_aux = 0, off_seq = 0, off_pos = 0;
     int sb_max = 16, aux_max = 16, max_n = 1;
     p->prefix.push_back(0);
     p->cprefix.push_back(0);
-    for (int b = 0; b < nbeams; b++) {
+    for (int si = 0; si < nbeams; si++) {
+        const int b = p->perm[si];
         const bsj_beam& bm = beams[b];
         if (bm.instance < 0 || bm.instance >= ninst) { delete p; return fail(ctx, BSJ_ERR_INVALID, "beam: instance index out of range"); }
         if (bm.mode < BSJ_MODE_V1 || bm.mode > BSJ_MODE_PMS) { delete p; return fail(ctx, BSJ_ERR_INVALID, "beam: unknown mode"); }
@@ -594,17 +607,17 @@ bsj_status plan_refresh(bsj_plan* p, int ninst, const bsj_instance* insts, const
         for (int64_t q = 0; q < (int64_t)insts[i].n * insts[i].m; q++)
             ops.push_back(((uint32_t)insts[i].duration[q] << 8) | (uint32_t)insts[i].machine[q]);
     std::fill(p->group_init.begin(), p->group_init.end(), INT32_MAX);
-    for (int b = 0; b < p->nseg; b++) {
-        const bsj_beam& bm = beams[b];
-        p->segs[b].seed = bm.seed;
+    for (int si = 0; si < p->nseg; si++) {
+        const bsj_beam& bm = beams[p->perm[si]];
+        p->segs[si].seed = bm.seed;
         SegState st{};
         st.P = 1;
         st.bound = bm.best_known;
         st.best = ~0ull;
         st.best_cmax = kSentinel;
         if (bm.mode > BSJ_MODE_CLEAN) glibc_rand_state(bm.seed, st.rng, &st.rng_i);
-        p->init[b] = st;
-        const int g = p->seg_group[b];
+        p->init[si] = st;
+        const int g = p->seg_group[si];
         p->group_init[g] = std::min(p->group_init[g], bm.best_known);
     }
     cudaStream_t st = ctx->stream;
@@ -628,10 +641,11 @@ struct RandCarry {
 // Start each ICH/PMS beam of the plan's next run from `in[b]` instead of its seed.
 bsj_status plan_put_rand(bsj_plan* p, const RandCarry* in)
 {
-    for (int b = 0; b < p->nseg; b++) {
-        if (p->segs[b].mode <= BSJ_MODE_CLEAN) continue;
-        p->init[b].rng_i = 34 + (in[b].i % 34);
-        std::memcpy(p->init[b].rng, in[b].r, sizeof(in[b].r));
+    for (int si = 0; si < p->nseg; si++) {
+        if (p->segs[si].mode <= BSJ_MODE_CLEAN) continue;
+        const RandCarry& c = in[p->perm[si]];
+        p->init[si].rng_i = 34 + (c.i % 34);
+        std::memcpy(p->init[si].rng, c.r, sizeof(c.r));
     }
     cudaStream_t st = p->ctx->stream;
     cudaError_t e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * p->nseg,
@@ -646,9 +660,10 @@ bsj_status plan_get_rand(bsj_plan* p, RandCarry* out)
     std::vector<SegState> st(p->nseg);
     cudaError_t e = cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(p->ctx, e, "rand state read");
-    for (int b = 0; b < p->nseg; b++) {
-        out[b].i = st[b].rng_i;
-        std::memcpy(out[b].r, st[b].rng, sizeof(out[b].r));
+    for (int si = 0; si < p->nseg; si++) {
+        RandCarry& c = out[p->perm[si]];
+        c.i = st[si].rng_i;
+        std::memcpy(c.r, st[si].rng, sizeof(c.r));
     }
     return BSJ_OK;
 }
@@ -792,21 +807,22 @@ bsj_status bsj_plan_results(bsj_plan* p, bsj_result* results)
     BSJ_CUDA(ctx, cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost));
     BSJ_CUDA(ctx, cudaMemcpy(grp.data(), p->d_group, sizeof(int32_t) * p->ngroups, cudaMemcpyDeviceToHost));
     bsj_status status = BSJ_OK;
-    for (int b = 0; b < p->nseg; b++) {
-        const SegDesc& d = p->segs[b];
+    for (int si = 0; si < p->nseg; si++) {
+        const SegDesc& d = p->segs[si];
+        const int b = p->perm[si];
         bsj_result& r = results[b];
-        r.makespan = st[b].makespan;
-        r.found = st[b].found;
-        r.expanded = st[b].expanded;
-        r.slots = st[b].slots;
-        r.levels = st[b].levels;
-        r.group_best = grp[p->seg_group[b]];
+        r.makespan = st[si].makespan;
+        r.found = st[si].found;
+        r.expanded = st[si].expanded;
+        r.slots = st[si].slots;
+        r.levels = st[si].levels;
+        r.group_best = grp[p->seg_group[si]];
         if (r.sequence) {
             BSJ_CUDA(ctx, cudaMemcpy(r.sequence, p->args.seq_pool + d.seq_off, sizeof(int32_t) * d.N, cudaMemcpyDeviceToHost));
         }
-        if (st[b].status != 0) {
+        if (st[si].status != 0) {
             status = BSJ_ERR_DEVICE;
-            ctx->err = "beam " + std::to_string(b) + ": device status " + std::to_string(st[b].status);
+            ctx->err = "beam " + std::to_string(b) + ": device status " + std::to_string(st[si].status);
         }
     }
     return status;
