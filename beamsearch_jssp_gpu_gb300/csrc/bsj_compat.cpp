@@ -16,7 +16,8 @@
 
 namespace {
 
-std::mutex g_mu;
+std::mutex g_mu;        // the context table
+std::mutex g_solve_mu;  // solves on the shared contexts
 std::vector<bsj_context*> g_ctx;  // one per device, created on first use
 
 bsj_context* device_context()
@@ -57,7 +58,13 @@ int run_mode(int mode, const JSSPInstance& inst, int beam_width, int best_known,
     bsj_result res{};
     res.sequence = seq.data();
     bsj_context* ctx = device_context();
-    bsj_status s = bsj_solve(ctx, &bi, &bb, &res, nullptr);
+    bsj_status s;
+    {
+        // one context per device is shared by every caller: calls are serialised (the
+        // reference's entry points are not re-entrant either, gpu/common/gpu_common.cuh:32)
+        std::lock_guard<std::mutex> lk(g_solve_mu);
+        s = bsj_solve(ctx, &bi, &bb, &res, nullptr);
+    }
     if (s != BSJ_OK) {
         std::fprintf(stderr, "CUDA error %s:%d  %s: %s\n", __FILE__, __LINE__, bsj_status_string(s),
                      bsj_last_error(ctx));

@@ -4,7 +4,9 @@
  * Plain C types only (no C++, no torch): pointers, sizes, status codes.  Every call
  * returns a bsj_status; no call exits the process.  Host pointers are borrowed for the
  * duration of the call.  A context owns one device, one stream by default and its device
- * memory; contexts are independent, so several may be used from different threads.
+ * memory; contexts are independent, so several may be used from different threads, but
+ * one context (and the plans made from it) is used by one thread at a time.  A server
+ * (bsj_server_*) is thread-safe.
  *
  * Reference interfaces these entry points replace (paths within bensdz/BeamSearch_JSSP_GPU):
  *   run_gpu_beam_search_v1   gpu/v1/solver.cuh:6-12, gpu/v1/solver.cu:178-298
@@ -208,7 +210,8 @@ typedef struct {
 } bsj_server_stats;
 /* cfg may be NULL (defaults). */
 bsj_status bsj_server_create(bsj_server **out, int device, const bsj_server_config *cfg);
-/* Drops queued requests, waits for running ones, frees everything. */
+/* Drops queued requests, waits for running ones, frees everything.  No other thread may
+   be inside a call on this server (a bsj_wait on a dropped request would never return). */
 void bsj_server_destroy(bsj_server *server);
 /* Copies the request and queues it.  BSJ_ERR_INVALID / BSJ_ERR_LIMIT as bsj_solve would
    return them, and BSJ_ERR_LIMIT when the request alone exceeds the memory budget. */

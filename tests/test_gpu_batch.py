@@ -92,3 +92,25 @@ def test_plan_rerun_is_deterministic(ctx):
         assert x["makespan"] == y["makespan"] and np.array_equal(x["seq"], y["seq"])
     assert plan.launches > 0
     plan.close()
+
+
+@pytest.mark.parametrize("groups", ["1", "3"])
+def test_beam_group_count_does_not_change_results(ctx, monkeypatch, groups):
+    """BSJ_MAX_BEAM_GROUPS (how many beam groups run as concurrent graph branches) and the
+    longest-first segment layout change scheduling only: every beam's result stays the
+    same, in the caller's order."""
+    rng = np.random.default_rng(9)
+    insts, beams = [], []
+    for k in range(10):
+        insts.append(synthetic_instance(int(rng.choice([5, 12, 20])), int(rng.choice([3, 6, 10])), 300 + k))
+        beams.append(BeamSpec(["v2", "clean", "v1", "pms"][k % 4], 64, 500000, 1000 + k, k, -1))
+    want = ctx.solve_batch(insts, beams)
+    monkeypatch.setenv("BSJ_MAX_BEAM_GROUPS", groups)
+    plan = ctx.plan(insts, beams)
+    plan.run()
+    got = plan.results()
+    plan.close()
+    for w, g, b in zip(want, got, beams):
+        assert g["makespan"] == w["makespan"], b
+        assert np.array_equal(g["seq"], w["seq"])
+        assert g["expanded"] == w["expanded"] and g["levels"] == w["levels"]
