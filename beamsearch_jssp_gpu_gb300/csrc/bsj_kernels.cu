@@ -47,6 +47,13 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Programmatic dependent launch: a level kernel launched with programmatic stream
+// serialization lets its successor be scheduled as soon as it starts (trigger), and waits
+// for its predecessor's completion and memory (wait) before touching anything the
+// predecessor writes.  Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Warp-wide asynchronous copy of one snapshot into shared memory (16-byte pieces).
 __device__ __forceinline__ void warp_prefetch(uint8_t* dst_smem, const uint8_t* src_gmem, int sbytes, int lane)
 {
@@ -370,7 +377,9 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32, NQ == 4 ? 3 : BSJ_STEP_
     // leave in slot order: ranks ascending, branches ascending
     unsigned long long* kstage = reinterpret_cast<unsigned long long*>(
         smem + (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * a.sb_max);
+    pdl_trigger();
     for (int k = threadIdx.x; k < 1000; k += blockDim.x) s_noise[k] = __ldg(a.noise + k);
+    pdl_wait();
     for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
         const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
         const SegDesc& d = a.segs[seg];
@@ -493,6 +502,8 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32, NQ == 4 ? 3 : BSJ_STEP_
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a, int s)
 {
+    pdl_trigger();
+    pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = gridDim.x * kWarpsPerStepCta;
     for (int flat = a.rank_lo + blockIdx.x * kWarpsPerStepCta + warp; flat < a.rank_hi; flat += nw) {
@@ -1482,6 +1493,8 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     __shared__ int s_cpref[kMaxChunks + 1];
     __shared__ int s_wsum[72];
     (void)sort_cap;
+    pdl_trigger();
+    pdl_wait();
     const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
     if (d.mode > MODE_CLEAN || s >= d.N) return;
@@ -1615,6 +1628,8 @@ struct Rng {
 // qn: quotient slots per staged parent (the batch's largest n; 0 when no beam is PMS).
 __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes, int qn)
 {
+    pdl_trigger();
+    pdl_wait();
     extern __shared__ __align__(16) uint8_t smem[];
     const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
@@ -1884,34 +1899,59 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
     return e;
 }
 
+#ifndef BSJ_PDL
+#define BSJ_PDL 1
+#endif
+
+// Launch with (pdl) or without programmatic stream serialization after the previous
+// kernel on the stream.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_kernel(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t stream,
+                                 bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    if (pdl && BSJ_PDL) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
     const size_t sm = step_smem_bytes(a.sb_max, a.max_n);
-    if (nq_mask & 2) k_step<1><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
-    if (nq_mask & 4) k_step<2><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
-    if (nq_mask & 16) k_step<4><<<grid, kWarpsPerStepCta * 32, sm, stream>>>(a, s);
-    return cudaGetLastError();
+    const int block = kWarpsPerStepCta * 32;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess && (nq_mask & 2)) e = launch_kernel(k_step<1>, grid, block, sm, stream, s >= 0, a, s);
+    if (e == cudaSuccess && (nq_mask & 4)) e = launch_kernel(k_step<2>, grid, block, sm, stream, s >= 0, a, s);
+    if (e == cudaSuccess && (nq_mask & 16)) e = launch_kernel(k_step<4>, grid, block, sm, stream, s >= 0, a, s);
+    return e;
 }
 
 cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream)
 {
-    k_gather_v1<<<grid, kWarpsPerStepCta * 32, 0, stream>>>(a, s);
-    return cudaGetLastError();
+    return launch_kernel(k_gather_v1, grid, kWarpsPerStepCta * 32, 0, stream, true, a, s);
 }
 
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream)
 {
-    k_select<<<a.seg_hi - a.seg_lo, kSelectThreads, select_smem_bytes(sort_cap), stream>>>(a, s, sort_cap);
-    return cudaGetLastError();
+    return launch_kernel(k_select, a.seg_hi - a.seg_lo, kSelectThreads, select_smem_bytes(sort_cap), stream, true,
+                         a, s, sort_cap);
 }
 
 cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes, int qn,
                         cudaStream_t stream)
 {
     const int q_bytes = chunk * qn * (int)sizeof(double);
-    k_heap<<<a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes, q_bytes), stream>>>(
-        a, s, chunk, stage_bytes, qn);
-    return cudaGetLastError();
+    return launch_kernel(k_heap, a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes, q_bytes),
+                         stream, true, a, s, chunk, stage_bytes, qn);
 }
 
 // The 1000 possible noise quotients of the gpu solvers' score, (float)(h % 1000) / 1e9f
