@@ -47,10 +47,13 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Programmatic dependent launch: a level kernel launched with programmatic stream
-// serialization lets its successor be scheduled as soon as it starts (trigger), and waits
-// for its predecessor's completion and memory (wait) before touching anything the
-// predecessor writes.  Without the launch attribute both instructions are no-ops.
+// Programmatic dependent launch.  The level kernels are launched with programmatic stream
+// serialization and wait (griddepcontrol.wait) for their predecessor's completion and
+// memory before touching anything it wrote.  k_step also lets its successor -- the next
+// level's one-CTA-per-beam select or heap -- be scheduled as soon as it starts, so that CTA
+// is resident when k_step ends.  The narrow kernels do not trigger early: the wide k_step
+// grid after them would sit on SM slots other beams need.  Without the launch attribute
+// both instructions are no-ops.
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
@@ -502,7 +505,6 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32, NQ == 4 ? 3 : BSJ_STEP_
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a, int s)
 {
-    pdl_trigger();
     pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = gridDim.x * kWarpsPerStepCta;
@@ -1493,7 +1495,6 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     __shared__ int s_cpref[kMaxChunks + 1];
     __shared__ int s_wsum[72];
     (void)sort_cap;
-    pdl_trigger();
     pdl_wait();
     const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
@@ -1628,7 +1629,6 @@ struct Rng {
 // qn: quotient slots per staged parent (the batch's largest n; 0 when no beam is PMS).
 __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes, int qn)
 {
-    pdl_trigger();
     pdl_wait();
     extern __shared__ __align__(16) uint8_t smem[];
     const int seg = a.seg_lo + blockIdx.x;
