@@ -36,7 +36,7 @@ constexpr int kMaxDuration = (1 << 24) - 1;
 constexpr int kSentinel = 500000;              // "no bound", gpu/v1/main.cu:57
 constexpr int kWarpsPerStepCta = 8;
 #ifndef BSJ_STEP_CHUNK
-#define BSJ_STEP_CHUNK 32
+#define BSJ_STEP_CHUNK 16
 #endif
 constexpr int kChunk = BSJ_STEP_CHUNK;                     // ranks per k_step work unit (8..32)
 constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;

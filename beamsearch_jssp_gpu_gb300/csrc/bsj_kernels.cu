@@ -367,8 +367,13 @@ template <int NQ>
 #ifndef BSJ_STEP_MIN_BLOCKS
 #define BSJ_STEP_MIN_BLOCKS 4
 #endif
+#ifndef BSJ_STEP_MIN_BLOCKS_NQ2
+#define BSJ_STEP_MIN_BLOCKS_NQ2 BSJ_STEP_MIN_BLOCKS
+#endif
 // four resident CTAs per SM (64 registers); the n > 64 instance needs more registers
-__global__ void __launch_bounds__(kWarpsPerStepCta * 32, NQ == 4 ? 3 : BSJ_STEP_MIN_BLOCKS) k_step(StepArgs a, int s)
+__global__ void __launch_bounds__(kWarpsPerStepCta * 32,
+                                  NQ == 4 ? 3 : NQ == 2 ? BSJ_STEP_MIN_BLOCKS_NQ2 : BSJ_STEP_MIN_BLOCKS)
+k_step(StepArgs a, int s)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ float s_noise[1000];
