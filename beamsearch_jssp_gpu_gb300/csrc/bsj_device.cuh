@@ -43,7 +43,8 @@ constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;
 constexpr int kMaxChunks = kMaxBeam / kChunk;
 static_assert(kChunk % kWarpsPerStepCta == 0 && kChunk <= 32, "a chunk is 1..4 ranks per warp");
 constexpr int kSelectThreads = 1024;
-constexpr int kHeapThreads = 64;
+constexpr int kHeapThreads = 256;    // k_heap: warp 0 runs the heap, warps 1..7 prepare chunks
+constexpr int kHeapMaxChunk = 32;     // parents per k_heap chunk (at most)
 
 // Device-side error bits (SegState::status).
 constexpr int kStatusBadLineage = 1;

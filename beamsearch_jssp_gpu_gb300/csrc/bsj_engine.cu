@@ -51,8 +51,8 @@ struct bsj_plan {
     int total_chunks = 0;
     int nq_mask = 0;
     int gather_grid = 1;
-    int sort_cap = 0, heap_k = 0, heap_chunk = 1, heap_stage = 16;
-    int heap_qn = 0;   // PMS quotient slots per staged parent (largest n; 0 without PMS beams)
+    int sort_cap = 0;
+    HeapCfg heap{0, 1, 16, 1};   // k_heap configuration (ICH/PMS beams)
     bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
     int step_grid = 1;
     // beam groups: contiguous beam ranges run as independent graph branches, so one
@@ -219,7 +219,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     // per-beam layout
     size_t off_beam = 0, off_slot = 0, off_keys = 0, off_sel = 0, off_mask = 0, off_hist = 0, off_kcnt = 0,
            off_aux = 0, off_seq = 0, off_pos = 0;
-    int sb_max = 16, aux_max = 16, max_n = 1;
+    int sb_max = 16, max_n = 1;
     p->prefix.push_back(0);
     p->cprefix.push_back(0);
     for (int si = 0; si < nbeams; si++) {
@@ -276,12 +276,16 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         p->cprefix.push_back(p->cprefix.back() + nch);
         sb_max = std::max(sb_max, d.sbytes);
         max_n = std::max(max_n, d.n);
-        aux_max = std::max(aux_max, d.auxbytes);
         p->maxN = std::max(p->maxN, d.N);
         if (d.mode == BSJ_MODE_V1) p->has_v1 = true;
         if (d.mode == BSJ_MODE_V1 || d.mode == BSJ_MODE_V2) p->has_zero = true;
         if (gpu) { p->has_gpu = true; p->sort_cap = std::max(p->sort_cap, d.K); }
-        else { p->has_compat = true; p->heap_k = std::max(p->heap_k, d.K); }
+        else {
+            p->has_compat = true;
+            p->heap.kmax = std::max(p->heap.kmax, d.K);
+            p->heap.ab = std::max(p->heap.ab, d.auxbytes);
+            p->heap.nmax = std::max(p->heap.nmax, d.n);
+        }
 
         SegState st{};
         st.P = 1;
@@ -301,17 +305,11 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         while (sc < p->sort_cap) sc <<= 1;
         p->sort_cap = sc;
     }
-    // ICH/PMS staging: two chunks of parents' child tables next to the heap
+    // ICH/PMS: the heap and the chunks of parents prepared ahead of it share the CTA's
+    // shared memory; the chunk is as many parents as fit (at most kHeapMaxChunk)
     if (p->has_compat) {
-        for (int b = 0; b < nbeams; b++)
-            if (p->segs[b].mode == BSJ_MODE_PMS) p->heap_qn = std::max(p->heap_qn, p->segs[b].n);
-        size_t budget = (size_t)ctx->max_smem_optin;
-        size_t base = heap_smem_bytes(p->heap_k, 0, 0);
-        const size_t per_parent = 2 * ((size_t)aux_max + sizeof(double) * p->heap_qn);
-        if (base + per_parent > budget) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "ICH/PMS beam too wide for shared memory"); }
-        int chunk = (int)std::min<size_t>(32, (budget - base) / per_parent);
-        p->heap_chunk = std::max(1, chunk);
-        p->heap_stage = p->heap_chunk * aux_max;
+        p->heap.chunk = heap_pick_chunk(p->heap, (size_t)ctx->max_smem_optin);
+        if (p->heap.chunk < 1) { delete p; return fail(ctx, BSJ_ERR_LIMIT, "ICH/PMS beam too wide for shared memory"); }
     }
     if (p->has_gpu && select_smem_bytes(p->sort_cap) > (size_t)ctx->max_smem_optin) {
         delete p;
@@ -412,8 +410,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         return cuda_fail(ctx, e, "plan upload");
     }
 
-    e = configure_kernels(std::max(p->sort_cap, 1), std::max(p->heap_k, 1), std::max(p->heap_stage, 16),
-                          p->heap_chunk * p->heap_qn * (int)sizeof(double), sb_max, max_n);
+    e = configure_kernels(std::max(p->sort_cap, 1), p->has_compat ? &p->heap : nullptr, sb_max, max_n);
     if (e != cudaSuccess) {
         cudaFree(p->mem);
         delete p;
@@ -545,7 +542,7 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
                 if (r != cudaSuccess) return r;
             }
             if (gr.has_compat) {
-                r = timed_g(2, [&] { return launch_heap(ga, lv, p->heap_k, p->heap_chunk, p->heap_stage, p->heap_qn, gs); });
+                r = timed_g(2, [&] { return launch_heap(ga, lv, p->heap, gs); });
                 if (r != cudaSuccess) return r;
             }
             if (lv < gr.maxN - 1) {

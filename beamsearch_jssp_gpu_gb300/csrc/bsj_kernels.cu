@@ -1539,29 +1539,80 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
 }
 
 // ------------------------------------------------------------------------------------
-// k_heap: ICH / PMS selection, serial per beam in the CPU solvers' order.  Thread 0
-// consumes the glibc rand() stream and runs the libstdc++ bounded-heap steps
-// (jssp_types.h:47-58) on shared memory; warp 1 stages the next parents' child tables.
+// k_heap: ICH / PMS selection per beam, in the CPU solvers' order (cpu/v0_ich/solver.cpp:
+// 22-39, cpu/v1_pms/solver.cpp:26-62, insert_into_beam jssp_types.h:47-58).
+//
+// The survivors and their order (the next level's parent order) are what libstdc++'s
+// bounded heap holds after every child has been offered in generation order, so the heap
+// stays serial: lane 0 of warp 0 runs it and nothing else.  Warps 1..7 work one chunk of
+// parents ahead of it:
+//   1. stage the chunk's child tables (written by k_step) in shared memory;
+//   2. consume the glibc rand() stream.  ICH draws one value per child, so the chunk's
+//      draws are known in advance and one warp generates them 31 at a time
+//      (warp_rand_fill).  BS-PMS draws a pivot and then one value per child on the pivot's
+//      machine, so one lane walks the parents, reading each position's machine count from
+//      a table the warps built with a histogram per parent;
+//   3. score every child (thread per child) and drop those the heap would reject anyway:
+//      once the heap is full its front only decreases, so a key that is not below a front
+//      published earlier is not below the front when its turn comes;
+//   4. compact the remaining children, in generation order, into the buffer the heap
+//      thread reads on its next pass.
 // ------------------------------------------------------------------------------------
-struct HeapSmem {
-    unsigned long long* hk;
-    uint32_t* hv;
-    uint32_t* ring;
-    uint8_t* stage;
+constexpr int kHeapProducers = kHeapThreads - 32;
+constexpr int kHeapProducerWarps = kHeapProducers / 32;
+constexpr int kHeapMiscBytes = 128 + kHeapProducerWarps * 64 * 4;
+
+__host__ __device__ __forceinline__ size_t hl_align(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// hk [K] u64 | hv [K] u32 | misc | per-parent coff [C+1], pm [C], rbase [C] | rb [34 + C(n+1)]
+// u32 | stage [C] child tables | cpar, cpos [C n] u8 | cdraw [C n] u32 | cntv [C n] u8 |
+// ck [2][C n] u64 | cv [2][C n] u32
+struct HeapLayout {
+    size_t hk, hv, misc, pp, rb, stage, cpar, cpos, cdraw, cntv, ck, cv, total;
+    __host__ __device__ explicit HeapLayout(const HeapCfg& c)
+    {
+        const size_t C = (size_t)c.chunk, cap = (size_t)c.chunk * (size_t)c.nmax;
+        size_t o = 0;
+        hk = o;
+        o += 8 * (size_t)c.kmax;
+        hv = o;
+        o = hl_align(o + 4 * (size_t)c.kmax);
+        misc = o;
+        o += kHeapMiscBytes;
+        pp = o;
+        o = hl_align(o + 4 * (3 * C + 1));
+        rb = o;
+        o = hl_align(o + 4 * (34 + C * ((size_t)c.nmax + 1)));
+        stage = o;
+        o = hl_align(o + C * (size_t)c.ab);
+        cpar = o;
+        o = hl_align(o + cap);
+        cpos = o;
+        o = hl_align(o + cap);
+        cdraw = o;
+        o = hl_align(o + 4 * cap);
+        cntv = o;
+        o = hl_align(o + cap);
+        ck = o;
+        o += 2 * 8 * cap;
+        cv = o;
+        o = hl_align(o + 2 * 4 * cap);
+        total = o;
+    }
 };
 
-// hk [K] u64 | hv [K] u32 | ring [64] u32 | misc [16] i32 | (16-aligned) stage [2][stage_bytes]
-// | quotients [2][q_bytes] (PMS: cmax / ns per staged child, as doubles)
-__host__ __device__ __forceinline__ size_t heap_stage_offset(int k)
+size_t heap_smem_bytes(const HeapCfg& c) { return HeapLayout(c).total; }
+
+int heap_pick_chunk(HeapCfg c, size_t budget)
 {
-    return (((size_t)k * 12 + 64 * 4 + 16 * 4) + 15) & ~(size_t)15;
+    for (int ch = kHeapMaxChunk; ch >= 1; ch--) {
+        c.chunk = ch;
+        if (heap_smem_bytes(c) <= budget) return ch;
+    }
+    return 0;
 }
 
-size_t heap_smem_bytes(int max_k, int stage_bytes, int q_bytes)
-{
-    return heap_stage_offset(max_k) + 2 * (size_t)stage_bytes + 2 * (size_t)q_bytes;
-}
-
+// libstdc++ __push_heap: the value rises from `hole` while its parent is smaller.
 __device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* hv, int hole, int top,
                                              unsigned long long vk, uint32_t vv)
 {
@@ -1576,6 +1627,8 @@ __device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* h
     hv[hole] = vv;
 }
 
+// libstdc++ __adjust_heap: the hole walks down to a leaf along the larger children (the
+// right one on ties, a lone left child is taken), then the value is pushed up from there.
 __device__ void heap_adjust(unsigned long long* hk, uint32_t* hv, int hole, int len,
                             unsigned long long vk, uint32_t vv)
 {
@@ -1597,42 +1650,32 @@ __device__ void heap_adjust(unsigned long long* hk, uint32_t* hv, int hole, int 
     heap_sift_up(hk, hv, hole, top, vk, vv);
 }
 
-// insert_into_beam (jssp_types.h:47-58) with push_heap / pop_heap semantics.
-__device__ __forceinline__ void heap_insert(unsigned long long* hk, uint32_t* hv, int& size, int K,
-                                            unsigned long long key, uint32_t val)
+// glibc rand() (TYPE_3): r[t] = r[t-31] + r[t-3] mod 2^32, rand() = r[t] >> 1.
+// rb[0..34) hold r[t0-34 .. t0-1]; writes r[t0 .. t0+cnt) to rb[34 ..).  Lane j makes
+// r[t+j] for 31 positions per step: unrolled, r[t+j] = sum over k of r[t+j-31-3k] (a
+// stride-3 inclusive prefix sum of the lanes' x_j = r[t+j-31]) + r[t-3+(j mod 3)].
+__device__ void warp_rand_fill(uint32_t* rb, int cnt, int lane)
 {
-    if (size < K) {
-        hk[size] = key;
-        hv[size] = val;
-        size++;
-        heap_sift_up(hk, hv, size - 1, 0, key, val);
-    } else if (key < hk[0]) {
-        if (size > 1) heap_adjust(hk, hv, 0, size - 1, hk[size - 1], hv[size - 1]);
-        hk[size - 1] = key;
-        hv[size - 1] = val;
-        heap_sift_up(hk, hv, size - 1, 0, key, val);
+    uint32_t x = lane < 31 ? rb[3 + lane] : 0u;
+    uint32_t b = rb[31 + lane % 3];
+    for (int t = 0; t < cnt; t += 31) {
+        uint32_t v = x, u;
+        u = __shfl_up_sync(FULL_MASK, v, 3);
+        if (lane >= 3) v += u;
+        u = __shfl_up_sync(FULL_MASK, v, 6);
+        if (lane >= 6) v += u;
+        u = __shfl_up_sync(FULL_MASK, v, 12);
+        if (lane >= 12) v += u;
+        u = __shfl_up_sync(FULL_MASK, v, 24);
+        if (lane >= 24) v += u;
+        v += b;
+        if (lane < 31 && t + lane < cnt) rb[34 + t + lane] = v;
+        x = v;
+        b = __shfl_sync(FULL_MASK, v, 28 + lane % 3);
     }
 }
 
-// glibc rand() stream: ring[34] holds r[i-34 .. i-1] at index (position mod 34); i is the
-// position of the next value, kept in [34, 68) so that no pass of any length overflows it.
-struct Rng {
-    uint32_t* ring;
-    uint32_t i;
-    __device__ __forceinline__ uint32_t next()
-    {
-        const uint32_t k = i - 34u;                     // i mod 34
-        const uint32_t a = k + 3u < 34u ? k + 3u : k + 3u - 34u;     // (i - 31) mod 34
-        const uint32_t b = k + 31u < 34u ? k + 31u : k + 31u - 34u;  // (i - 3) mod 34
-        const uint32_t v = ring[a] + ring[b];
-        ring[k] = v;
-        i = (k == 33u) ? 34u : i + 1u;
-        return v >> 1;
-    }
-};
-
-// qn: quotient slots per staged parent (the batch's largest n; 0 when no beam is PMS).
-__global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int chunk, int stage_bytes, int qn)
+__global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, HeapCfg cfg)
 {
     pdl_wait();
     extern __shared__ __align__(16) uint8_t smem[];
@@ -1640,142 +1683,327 @@ __global__ void __launch_bounds__(kHeapThreads) k_heap(StepArgs a, int s, int ch
     const SegDesc& d = a.segs[seg];
     if (d.mode < MODE_ICH || s >= d.N) return;
     SegState& st = a.st[seg];
+    const HeapLayout HL(cfg);
+    unsigned long long* hk = reinterpret_cast<unsigned long long*>(smem + HL.hk);
+    uint32_t* hv = reinterpret_cast<uint32_t*>(smem + HL.hv);
+    uint8_t* misc = smem + HL.misc;
+    unsigned long long* s_front = reinterpret_cast<unsigned long long*>(misc);      // published heap front
+    unsigned long long* s_best = reinterpret_cast<unsigned long long*>(misc + 8);   // (cmax << 32 | ref) min
+    int* s_cnt = reinterpret_cast<int*>(misc + 16);                                 // [2] kept children
+    int* s_wsum = reinterpret_cast<int*>(misc + 24);                                // [8] per-warp counts
+    int* s_dtot = reinterpret_cast<int*>(misc + 56);                                // draws so far
+    int* s_draws = reinterpret_cast<int*>(misc + 60);                               // draws of a chunk
+    int* s_size = reinterpret_cast<int*>(misc + 64);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(misc + 128);                       // [warps][64]
+    const int C = cfg.chunk;
+    int* coff = reinterpret_cast<int*>(smem + HL.pp);  // [C+1] first child of each parent
+    int* pm = coff + C + 1;                            // [C] BS-PMS pivot machine
+    int* rbase = pm + C;                               // [C] BS-PMS first noise draw (rb index)
+    uint32_t* rb = reinterpret_cast<uint32_t*>(smem + HL.rb);
+    uint8_t* stage = smem + HL.stage;
+    uint8_t* cpar = smem + HL.cpar;
+    uint8_t* cpos = smem + HL.cpos;
+    uint32_t* cdraw = reinterpret_cast<uint32_t*>(smem + HL.cdraw);
+    uint8_t* cntv = smem + HL.cntv;
+    const size_t cap = (size_t)C * cfg.nmax;
+    unsigned long long* ck = reinterpret_cast<unsigned long long*>(smem + HL.ck);
+    uint32_t* cv = reinterpret_cast<uint32_t*>(smem + HL.cv);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = d.K, n = d.n, ab = d.auxbytes;
-    HeapSmem H;
-    H.hk = reinterpret_cast<unsigned long long*>(smem);
-    H.hv = reinterpret_cast<uint32_t*>(H.hk + K);
-    H.ring = H.hv + K;
-    int* hmisc = reinterpret_cast<int*>(H.ring + 64);
-    H.stage = smem + heap_stage_offset(K);
-    const int tid = threadIdx.x;
     const int P = st.P;
     const uint8_t* aux = a.aux_pool + d.aux_off;
-    if (tid < 34) H.ring[tid] = st.rng[tid];
-
-    // chunk 0 staged by everyone
-    const int nchunks = (P + chunk - 1) / chunk;
-    const bool pms = (d.mode == MODE_PMS) && qn >= n;
-    double* qbuf = reinterpret_cast<double*>(H.stage + 2 * (size_t)stage_bytes);
-    auto stage_chunk = [&](int q, int t0, int nt) {
-        if (q >= nchunks) return;
-        const int c0 = q * chunk;
-        const int cnt = (P - c0) < chunk ? (P - c0) : chunk;
-        const uint4* src = reinterpret_cast<const uint4*>(aux + (int64_t)c0 * ab);
-        uint4* dst = reinterpret_cast<uint4*>(H.stage + (size_t)(q & 1) * stage_bytes);
-        for (int u = t0; u < (cnt * ab) >> 4; u += nt) dst[u] = src[u];
-    };
-    // BS-PMS score's first quotient, cmax / ns (cpu/v1_pms/solver.cpp:52), for every ready
-    // position of the staged parents, off the serial thread (the pivot is not drawn yet)
-    auto quotients = [&](int q, int t0, int nt) {
-        if (!pms || q >= nchunks) return;
-        const int c0 = q * chunk;
-        const int cnt = (P - c0) < chunk ? (P - c0) : chunk;
-        const uint8_t* sbuf = H.stage + (size_t)(q & 1) * stage_bytes;
-        double* qb = qbuf + (size_t)(q & 1) * chunk * qn;
-        const double ns = (double)(s + 1);
-        for (int u = t0; u < cnt * n; u += nt) {
-            const int cl = u / n, i = u - cl * n;
-            const uint8_t* pa = sbuf + (size_t)cl * ab;
-            if (i < (int)*reinterpret_cast<const uint32_t*>(pa))
-                qb[cl * qn + i] = __ddiv_rn((double)reinterpret_cast<const int32_t*>(pa + 4)[i], ns);
-        }
-    };
-    stage_chunk(0, tid, blockDim.x);
-    __syncthreads();
-    quotients(0, tid, blockDim.x);
-    __syncthreads();
-
-    int size = 0;
-    int best_cm = kSentinel;
-    uint32_t best_ref = 0;
-    long long gen = 0;
-    const int bound = st.bound;
     const bool ich = (d.mode == MODE_ICH);
     const bool last = (s == d.N - 1);
-    Rng g;
-    g.ring = H.ring;
-    g.i = st.rng_i;
+    const int bound = st.bound;
+    const uint32_t k0 = st.rng_i - 34u;
+    const int nchunks = (P + C - 1) / C;
+    if (tid == 0) {
+        *s_front = ~0ull;
+        *s_best = ~0ull;
+        *s_dtot = 0;
+    }
+    if (tid < 34) rb[tid] = st.rng[(k0 + (uint32_t)tid) % 34u];
+    __syncthreads();
 
-    for (int q = 0; q < nchunks; q++) {
-        if (tid >= 32) {
-            stage_chunk(q + 1, tid - 32, blockDim.x - 32);
-            __syncwarp();
-            quotients(q + 1, tid - 32, blockDim.x - 32);
-        } else if (tid == 0) {
-            const int c0 = q * chunk;
-            const int cend = (P - c0) < chunk ? P : c0 + chunk;
-            const uint8_t* sbuf = H.stage + (size_t)(q & 1) * stage_bytes;
-            for (int c = c0; c < cend; c++) {
-                const uint8_t* pa = sbuf + (size_t)(c - c0) * ab;
-                const int rc = (int)*reinterpret_cast<const uint32_t*>(pa);
-                const int32_t* cc = reinterpret_cast<const int32_t*>(pa + 4);
-                const uint8_t* cmv = pa + 4 + 4 * n;
-                const uint8_t* jb = pa + 4 + 5 * n;
-                if (ich) {
-                    // cpu/v0_ich/solver.cpp:24-39: score = cmax + (rand()%100)*0.01; the pair
-                    // (cmax, rand()%100) orders exactly like that double
-                    for (int i = 0; i < rc; i++) {
-                        const uint32_t dr = g.next();
-                        const unsigned long long key = (unsigned long long)cc[i] * 100ull + (dr % 100u);
-                        heap_insert(H.hk, H.hv, size, K, key, ((uint32_t)c << 8) | (uint32_t)i);
+    const int pt = tid - 32, pw = warp - 1;
+    long long gen = 0;
+    auto pbar = [] { asm volatile("bar.sync 1, %0;" ::"r"(kHeapProducers) : "memory"); };
+    auto produce = [&](int q) {
+        if (q >= nchunks) return;
+        const int c0 = q * C;
+        const int cnt = (P - c0) < C ? (P - c0) : C;
+        {
+            const uint4* s4 = reinterpret_cast<const uint4*>(aux + (int64_t)c0 * ab);
+            uint4* d4 = reinterpret_cast<uint4*>(stage);
+            for (int u = pt; u < (cnt * ab) >> 4; u += kHeapProducers) d4[u] = __ldcg(s4 + u);
+        }
+        pbar();
+        auto rc_of = [&](int p) { return (int)*reinterpret_cast<const uint32_t*>(stage + (size_t)p * ab); };
+        auto cc_of = [&](int p) { return reinterpret_cast<const int32_t*>(stage + (size_t)p * ab + 4); };
+        auto mc_of = [&](int p) { return stage + (size_t)p * ab + 4 + 4 * n; };
+        if (ich) {
+            if (pw == 0) {
+                // cpu/v0_ich/solver.cpp:22-35: one draw per child, parents in order
+                const int v = lane < cnt ? rc_of(lane) : 0;
+                int x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL_MASK, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane < cnt) coff[lane] = x - v;
+                const int T = __shfl_sync(FULL_MASK, x, 31);
+                if (lane == 0) {
+                    coff[cnt] = T;
+                    *s_draws = T;
+                }
+                warp_rand_fill(rb, T, lane);
+            }
+            pbar();
+        } else {
+            // machines' ready-op counts per ready position (histogram per parent)
+            uint32_t* wh = hist + pw * 64;
+            for (int p = pw; p < cnt; p += kHeapProducerWarps) {
+                const int rc = rc_of(p);
+                const uint8_t* mc = mc_of(p);
+                wh[lane] = 0;
+                wh[lane + 32] = 0;
+                __syncwarp();
+                for (int i = lane; i < rc; i += 32) atomicAdd(&wh[mc[i]], 1u);
+                __syncwarp();
+                for (int i = lane; i < rc; i += 32) cntv[p * n + i] = (uint8_t)wh[mc[i]];
+                __syncwarp();
+            }
+            pbar();
+            if (pt == 0) {
+                // cpu/v1_pms/solver.cpp:26-53: a parent with ready ops draws its pivot, then one
+                // noise value per ready op on the pivot's machine, in ready-list order
+                int pos = 34, k = 0;
+                uint32_t r3 = rb[31], r2 = rb[32], r1 = rb[33];
+                for (int p = 0; p < cnt; p++) {
+                    const int rc = rc_of(p);
+                    coff[p] = k;
+                    rbase[p] = pos;
+                    if (rc == 0) {
+                        pm[p] = -1;
+                        continue;
                     }
-                    gen += rc;
-                } else if (rc > 0) {
-                    // cpu/v1_pms/solver.cpp:30-62
-                    const uint32_t dp = g.next();
-                    const int target = cmv[dp % (uint32_t)rc];
-                    for (int i = 0; i < rc; i++) {
-                        if (cmv[i] != target) continue;
-                        const uint32_t dn = g.next();
-                        const double qv = pms ? qbuf[(size_t)(q & 1) * chunk * qn + (c - c0) * qn + i]
-                                              : __ddiv_rn((double)cc[i], (double)(s + 1));
-                        const double sc = __dadd_rn(qv, a.dnoise[dn % 1000u]);
-                        gen++;
-                        if (last && cc[i] < best_cm) {
-                            best_cm = cc[i];
-                            best_ref = ((uint32_t)c << 8) | (uint32_t)jb[i];
-                        }
-                        if (cc[i] < bound)
-                            heap_insert(H.hk, H.hv, size, K, (unsigned long long)__double_as_longlong(sc),
-                                        ((uint32_t)c << 8) | (uint32_t)i);
+                    uint32_t v = rb[pos - 31] + r3;
+                    rb[pos++] = v;
+                    r3 = r2; r2 = r1; r1 = v;
+                    const int piv = (int)((v >> 1) % (uint32_t)rc);
+                    pm[p] = mc_of(p)[piv];
+                    const int c = cntv[p * n + piv];
+                    rbase[p] = pos;
+                    for (int j = 0; j < c; j++) {
+                        v = rb[pos - 31] + r3;
+                        rb[pos++] = v;
+                        r3 = r2; r2 = r1; r1 = v;
                     }
+                    k += c;
+                }
+                coff[cnt] = k;
+                *s_draws = pos - 34;
+            }
+            pbar();
+        }
+        const int T = coff[cnt];
+        const int D = *s_draws;
+        // children in generation order: parent, ready position, its draw
+        for (int p = pw; p < cnt; p += kHeapProducerWarps) {
+            const int rc = rc_of(p);
+            const int base = coff[p];
+            if (ich) {
+                for (int i = lane; i < rc; i += 32) {
+                    const int k = base + i;
+                    cpar[k] = (uint8_t)p;
+                    cpos[k] = (uint8_t)i;
+                    cdraw[k] = rb[34 + k];
+                }
+            } else {
+                const int pmach = pm[p];
+                const uint8_t* mc = mc_of(p);
+                const int r0 = rbase[p];
+                int carry = 0;
+                for (int i0 = 0; i0 < rc; i0 += 32) {
+                    const int i = i0 + lane;
+                    const bool on = i < rc && (int)mc[i] == pmach;
+                    const uint32_t bal = __ballot_sync(FULL_MASK, on);
+                    if (on) {
+                        const int r = carry + __popc(bal & ((1u << lane) - 1u));
+                        cpar[base + r] = (uint8_t)p;
+                        cpos[base + r] = (uint8_t)i;
+                        cdraw[base + r] = rb[r0 + r];
+                    }
+                    carry += __popc(bal);
                 }
             }
         }
-        __syncthreads();
-    }
-
-    if (tid == 0) {
-        hmisc[0] = size;
-        st.rng_i = g.i;
-        st.expanded += gen;
-        st.slots += gen;
-        if (P > 0) st.levels += 1;
-        st.P = size;
-        if (!last) st.materialized += size;
-        if (last) {
-            if (ich) {
-                // min makespan over the final beam, first in array order (v0_ich :47-51)
-                for (int r = 0; r < size; r++) {
-                    const uint32_t e = H.hv[r];
-                    const int c = (int)(e >> 8), i = (int)(e & 0xFFu);
-                    const uint8_t* pa = aux + (int64_t)c * ab;
-                    const int cm = reinterpret_cast<const int32_t*>(pa + 4)[i];
-                    if (cm < best_cm) {
-                        best_cm = cm;
-                        best_ref = ((uint32_t)c << 8) | (uint32_t)pa[4 + 5 * n + i];
+        pbar();
+        // score, drop what the heap would reject, compact in order
+        const double ns = (double)(s + 1);
+        unsigned long long bmin = ~0ull;
+        unsigned long long* okey = ck + (size_t)(q & 1) * cap;
+        uint32_t* oval = cv + (size_t)(q & 1) * cap;
+        int out = 0;
+        for (int t0 = 0; t0 < T; t0 += kHeapProducers) {
+            const int k = t0 + pt;
+            bool keep = false;
+            unsigned long long key = 0;
+            uint32_t val = 0;
+            if (k < T) {
+                const int p = cpar[k], i = cpos[k];
+                const int cc = cc_of(p)[i];
+                const uint32_t dr = cdraw[k] >> 1;
+                const unsigned long long F = *reinterpret_cast<volatile unsigned long long*>(s_front);
+                if (ich) {
+                    // score = cmax + (rand()%100)*0.01 (cpu/v0_ich/solver.cpp:35): the pair
+                    // (cmax, rand()%100) orders exactly like that double
+                    key = (unsigned long long)cc * 100ull + (dr % 100u);
+                    keep = key < F;
+                } else {
+                    // cpu/v1_pms/solver.cpp:52-57
+                    const double sc = __dadd_rn(__ddiv_rn((double)cc, ns), a.dnoise[dr % 1000u]);
+                    key = (unsigned long long)__double_as_longlong(sc);
+                    keep = cc < bound && key < F;
+                    if (last && cc < kSentinel) {
+                        const unsigned long long bk = ((unsigned long long)(uint32_t)cc << 32) |
+                                                      ((unsigned long long)(c0 + p) << 8) | (unsigned)i;
+                        bmin = bk < bmin ? bk : bmin;
                     }
                 }
+                val = ((uint32_t)(c0 + p) << 8) | (uint32_t)i;
+            }
+            const uint32_t bal = __ballot_sync(FULL_MASK, keep);
+            if (lane == 0) s_wsum[pw] = __popc(bal);
+            pbar();
+            int off = out, tot = 0;
+#pragma unroll
+            for (int w = 0; w < kHeapProducerWarps; w++) {
+                const int x = s_wsum[w];
+                off += (w < pw) ? x : 0;
+                tot += x;
+            }
+            if (keep) {
+                const int o = off + __popc(bal & ((1u << lane) - 1u));
+                okey[o] = key;
+                oval[o] = val;
+            }
+            out += tot;
+            pbar();
+        }
+        if (last && !ich) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long y = __shfl_xor_sync(FULL_MASK, bmin, o);
+                bmin = y < bmin ? y : bmin;
+            }
+            if (lane == 0 && bmin != ~0ull) atomicMin(s_best, bmin);
+        }
+        if (pt == 0) {
+            s_cnt[q & 1] = out;
+            gen += T;
+        }
+        // the stream's last 34 values are the next chunk's history
+        const uint32_t hold = pt < 34 ? rb[D + pt] : 0u;
+        pbar();
+        if (pt < 34) rb[pt] = hold;
+        if (pt == 0) *s_dtot += D;
+    };
+
+    if (warp > 0) produce(0);
+    __syncthreads();
+    int size = 0;
+    unsigned long long front = ~0ull;
+    for (int q = 0; q < nchunks; q++) {
+        if (warp > 0) {
+            produce(q + 1);
+        } else if (lane == 0) {
+            // insert_into_beam (jssp_types.h:47-58): push while below K, else replace the
+            // front (pop_heap, overwrite the back, push_heap) when strictly better
+            const int nc = s_cnt[q & 1];
+            const unsigned long long* ik = ck + (size_t)(q & 1) * cap;
+            const uint32_t* iv = cv + (size_t)(q & 1) * cap;
+            unsigned long long nkey = nc > 0 ? ik[0] : 0ull;
+            uint32_t nval = nc > 0 ? iv[0] : 0u;
+            for (int k = 0; k < nc; k++) {
+                const unsigned long long key = nkey;
+                const uint32_t val = nval;
+                if (k + 1 < nc) {
+                    nkey = ik[k + 1];
+                    nval = iv[k + 1];
+                }
+                if (size < K) {
+                    heap_sift_up(hk, hv, size, 0, key, val);
+                    if (++size == K) {
+                        front = hk[0];
+                        *reinterpret_cast<volatile unsigned long long*>(s_front) = front;
+                    }
+                } else if (key < front) {
+                    if (size > 1) heap_adjust(hk, hv, 0, size - 1, hk[size - 1], hv[size - 1]);
+                    heap_sift_up(hk, hv, size - 1, 0, key, val);
+                    front = hk[0];
+                    *reinterpret_cast<volatile unsigned long long*>(s_front) = front;
+                }
+            }
+            *s_size = size;
+        }
+        __syncthreads();
+    }
+    if (nchunks == 0 && tid == 0) *s_size = 0;
+    if (tid == 32) {
+        st.expanded += gen;
+        st.slots += gen;
+    }
+    if (last && ich) {
+        // min makespan over the final beam, first in array order (cpu/v0_ich/solver.cpp:47-51)
+        __syncthreads();
+        const int fs = *s_size;
+        unsigned long long bmin = ~0ull;
+        for (int r = tid; r < fs; r += blockDim.x) {
+            const uint32_t e = hv[r];
+            const uint8_t* pa = aux + (int64_t)(e >> 8) * ab;
+            const int cm = reinterpret_cast<const int32_t*>(pa + 4)[e & 0xFFu];
+            if (cm < kSentinel) {
+                const unsigned long long bk = ((unsigned long long)(uint32_t)cm << 32) | (unsigned)r;
+                bmin = bk < bmin ? bk : bmin;
+            }
+        }
+        if (bmin != ~0ull) atomicMin(s_best, bmin);
+    }
+    __syncthreads();
+    const int out_size = *s_size;
+    if (tid == 0) {
+        const uint32_t dt = (uint32_t)*s_dtot;
+        st.rng_i = 34u + (k0 + dt) % 34u;
+        if (P > 0) st.levels += 1;
+        st.P = out_size;
+        if (!last) st.materialized += out_size;
+        if (last) {
+            int best_cm = kSentinel;
+            uint32_t best_ref = 0;
+            const unsigned long long b = *s_best;
+            if (b != ~0ull) {
+                best_cm = (int)(b >> 32);
+                uint32_t c, i;
+                if (ich) {
+                    const uint32_t e = hv[(uint32_t)b];
+                    c = e >> 8;
+                    i = e & 0xFFu;
+                } else {
+                    c = (uint32_t)(b >> 8) & 0xFFFFFFu;
+                    i = (uint32_t)b & 0xFFu;
+                }
+                best_ref = (c << 8) | (uint32_t)aux[(int64_t)c * ab + 4 + 5 * n + i];
             }
             st.best_cmax = best_cm;
             st.best_ref = best_ref;
         }
     }
-    __syncthreads();
-    if (tid < 34) st.rng[tid] = H.ring[tid];
-    const int out_size = hmisc[0];
+    if (tid < 34) st.rng[(k0 + (uint32_t)*s_dtot + (uint32_t)tid) % 34u] = rb[tid];
     uint32_t* sel = a.sel + d.sel_off;
-    for (int r = tid; r < out_size; r += blockDim.x) sel[r] = H.hv[r];
+    for (int r = tid; r < out_size; r += blockDim.x) sel[r] = hv[r];
 }
 
 // ------------------------------------------------------------------------------------
@@ -1882,12 +2110,12 @@ static cudaError_t raise_smem(F* fn, size_t bytes)
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int q_bytes, int sb_max, int max_n)
+cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int max_n)
 {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = set_carveout();
     if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e == cudaSuccess) e = raise_smem(k_heap, heap_smem_bytes(max_k, stage_bytes, q_bytes));
+    if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
     if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
     if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
     if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
@@ -1951,12 +2179,9 @@ cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t s
                          a, s, sort_cap);
 }
 
-cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes, int qn,
-                        cudaStream_t stream)
+cudaError_t launch_heap(const StepArgs& a, int s, const HeapCfg& hc, cudaStream_t stream)
 {
-    const int q_bytes = chunk * qn * (int)sizeof(double);
-    return launch_kernel(k_heap, a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(max_k, stage_bytes, q_bytes),
-                         stream, true, a, s, chunk, stage_bytes, qn);
+    return launch_kernel(k_heap, a.seg_hi - a.seg_lo, kHeapThreads, heap_smem_bytes(hc), stream, true, a, s, hc);
 }
 
 // The 1000 possible noise quotients of the gpu solvers' score, (float)(h % 1000) / 1e9f

@@ -41,10 +41,18 @@ struct StepArgs {
     const double* dnoise;         // [1000]: (double)k / 1e6 (BS-PMS noise), IEEE round-to-nearest
 };
 
+// k_heap launch configuration: the largest K, child-table row (bytes) and n of the
+// launch's ICH/PMS beams, and the parents prepared per chunk.
+struct HeapCfg {
+    int32_t kmax, chunk, ab, nmax;
+};
+
 // Grid / shared-memory sizing helpers.
 size_t step_smem_bytes(int sb_max, int max_n);
 size_t select_smem_bytes(int sort_cap);
-size_t heap_smem_bytes(int max_k, int stage_bytes, int q_bytes);
+size_t heap_smem_bytes(const HeapCfg& c);
+// Largest chunk in [1, kHeapMaxChunk] whose k_heap shared memory fits `budget`; 0 if none.
+int heap_pick_chunk(HeapCfg c, size_t budget);
 
 // Launchers (asynchronous on `stream`).
 // k_step is instantiated per NQ = ceil(n/32) in {1, 2, 4}; nq_mask has bit NQ set for
@@ -53,12 +61,11 @@ cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStr
 int nq_class(int n);
 cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream);
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream);
-cudaError_t launch_heap(const StepArgs& a, int s, int max_k, int chunk, int stage_bytes, int qn,
-                        cudaStream_t stream);
+cudaError_t launch_heap(const StepArgs& a, int s, const HeapCfg& hc, cudaStream_t stream);
 // Fills noise[0..1000) with (float)k / 1e9f (once per plan; k_step copies it per CTA).
 cudaError_t launch_noise_table(float* noise, double* dnoise, cudaStream_t stream);
 cudaError_t launch_finalize(const StepArgs& a, cudaStream_t stream);
-cudaError_t configure_kernels(int sort_cap, int max_k, int stage_bytes, int q_bytes, int sb_max, int max_n);
+cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int max_n);
 // Raise (never lower) the dynamic shared-memory limits of k_select and k_step to what
 // a launch with `sort_cap` / `sb_max` needs.
 cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n);

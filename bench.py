@@ -16,6 +16,8 @@ Arms:
                      per beam on the host cores, each step a bounded sample of levels.
 
 Also on the JSON line (rank 0; --no-extras skips them):
+  "pms_exact" the same 8 beams in BS-PMS mode (the reference CPU solver's exact semantics,
+             serial bounded heap per beam), candidates/s and makespans;
   "batched"  256 synthetic instances of uneven size (n in {10..100}, m in {5..20},
              K in {256..4096}) in one bsj_solve_batch, solves/s against the same
              instances solved one call at a time (the plain path), makespans compared;
@@ -307,6 +309,7 @@ def gpu_arm(args) -> int:
 
     extras = {}
     if rank == 0 and not args.no_extras:
+        extras["pms_exact"] = pms_exact(ctx, mc, du, stream)
         extras["batched"] = batched_stream(ctx)
         extras["serving"] = served_stream(ctx, local)
 
@@ -329,8 +332,36 @@ def gpu_arm(args) -> int:
 
 
 # ------------------------------------------------------------------------------------
-# Batched and served streams (rank 0, after the headline measurement)
+# BS-PMS exact mode, batched and served streams (rank 0, after the headline measurement)
 # ------------------------------------------------------------------------------------
+def pms_exact(ctx, mc, du, stream) -> dict:
+    """The headline's 8 beams in BS-PMS mode (cpu/v1_pms/solver.cpp semantics: glibc rand()
+    pivots and noise, fp64 score, libstdc++ bounded heap; makespans equal to the reference's
+    CPU solver for the same srand seeds 0-7, which are the cpu_baseline's seeds).  The heap
+    is serial per beam (k_heap), so this is one search per SM, not the throughput path."""
+    import torch
+
+    from beamsearch_jssp_gpu_gb300 import BeamSpec
+
+    beams = [BeamSpec("pms", K, 500000, sd, 0, 0) for sd in range(BEAMS)]
+    plan = ctx.plan([(mc, du)], beams)
+    plan.run(stream.cuda_stream)
+    plan.results(with_sequence=False)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.run(stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    res = plan.results(with_sequence=False)
+    plan.close()
+    expanded = sum(r["expanded"] for r in res)
+    return {"workload": f"{BEAMS} beams, BS-PMS mode, {N_JOBS}x{N_MACH}, K={K}, srand seeds 0-{BEAMS - 1}",
+            "expanded_per_s": expanded / (ms / 1000.0), "ms_per_search": ms,
+            "makespans": [r["makespan"] for r in res]}
+
+
 def batched_stream(ctx, count: int = 256, seed: int = 1) -> dict:
     """256 synthetic instances of uneven size in one set of launches (bsj_solve_batch),
     against the plain path: the same instances solved one call at a time (bsj_solve)."""
