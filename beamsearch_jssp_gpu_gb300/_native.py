@@ -33,7 +33,10 @@ EXPORTED = [
     "bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count",
     "bsj_plan_estimate", "bsj_plan_device_bytes", "bsj_plan_update",
     "bsj_server_create", "bsj_server_destroy", "bsj_submit", "bsj_poll", "bsj_wait", "bsj_server_get_stats",
+    "bsj_plan_autotune", "bsj_plan_set_chunk", "bsj_plan_chunk", "bsj_set_autotune",
 ]
+CHUNK_SIZES = (8, 16, 32)  # k_step work-unit sizes (survivors per thread block)
+CHUNK_CANDIDATES = (0, 8, 16, 32)  # what the autotuner chooses among: 0 = the default rule
 
 
 class ServerConfig(ctypes.Structure):
@@ -120,6 +123,12 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
                                  P(ctypes.c_int64), P(ctypes.c_int64)]
     L.bsj_plan_set_timing.argtypes = [vp, ctypes.c_int]
     L.bsj_plan_kernel_ms.argtypes = [vp, P(ctypes.c_float), P(ctypes.c_int64), ctypes.c_int]
+    # autotuning of the k_step chunk size
+    L.bsj_plan_autotune.argtypes = [vp, vp, ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_float)]
+    L.bsj_plan_set_chunk.argtypes = [vp, ctypes.c_int32]
+    L.bsj_plan_chunk.argtypes = [vp]
+    L.bsj_plan_chunk.restype = ctypes.c_int32
+    L.bsj_set_autotune.argtypes = [vp, ctypes.c_int32]
     # allocation-free single-beam solve: device pointers in and out (include/bsj.h)
     L.bsj_solve_noalloc.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int32, ctypes.c_uint32, vp, vp]
@@ -150,7 +159,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
                  "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
-                 "bsj_plan_set_timing", "bsj_plan_kernel_ms"):
+                 "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_plan_autotune", "bsj_plan_set_chunk",
+                 "bsj_set_autotune"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

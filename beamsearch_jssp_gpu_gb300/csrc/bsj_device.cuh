@@ -35,13 +35,17 @@ constexpr int kMaxBeam = 16384;
 constexpr int kMaxDuration = (1 << 24) - 1;
 constexpr int kSentinel = 500000;              // "no bound", gpu/v1/main.cu:57
 constexpr int kWarpsPerStepCta = 8;
-#ifndef BSJ_STEP_CHUNK
-#define BSJ_STEP_CHUNK 16
-#endif
-constexpr int kChunk = BSJ_STEP_CHUNK;                     // ranks per k_step work unit (8..32)
-constexpr int kRanksPerWarp = kChunk / kWarpsPerStepCta;
-constexpr int kMaxChunks = kMaxBeam / kChunk;
-static_assert(kChunk % kWarpsPerStepCta == 0 && kChunk <= 32, "a chunk is 1..4 ranks per warp");
+// k_step work unit: a chunk of consecutive ranks of one beam per CTA, 1, 2 or 4 ranks per
+// warp.  The chunk size is chosen per plan (StepArgs::chunk) among kChunkSizes, by the
+// autotuner or by the default rule; candidate keys and per-chunk counts are laid out for
+// every size (keys for the largest, counts for the smallest).
+constexpr int kNumChunkSizes = 3;
+constexpr int kChunkSizes[kNumChunkSizes] = {8, 16, 32};
+constexpr int kMinChunk = 8;
+constexpr int kMaxChunk = 32;
+constexpr int kDefaultChunk = 16;   // ranks per k_step CTA when nothing else decides
+constexpr int kMaxChunks = kMaxBeam / kMinChunk;
+static_assert(kMinChunk % kWarpsPerStepCta == 0 && kMaxChunk <= 32, "a chunk is 1..4 ranks per warp");
 constexpr int kSelectThreads = 1024;
 constexpr int kHeapThreads = 256;    // k_heap: warp 0 runs the heap, warps 1..7 prepare chunks
 constexpr int kHeapMaxChunk = 32;     // parents per k_heap chunk (at most)

@@ -41,6 +41,7 @@ struct bsj_context {
     // plans of recent batch shapes (most recent last), reused with new data
     std::vector<std::pair<std::string, bsj_plan*>> cache;
     uint64_t hits = 0;
+    bool autotune = false;  // tune each new batch shape on its first bsj_solve_batch
 };
 
 struct bsj_plan {
@@ -48,18 +49,24 @@ struct bsj_plan {
     int nseg = 0, ninst = 0, ngroups = 0;
     int maxN = 0;
     int total_ranks = 0;
-    int total_chunks = 0;
     int nq_mask = 0;
+    // k_step work unit (survivors per CTA): variant 0 runs every group with the chunk size
+    // the default rule gives it (Group::rule_var), variant 1 + v every group with
+    // kChunkSizes[v].  Set by the default, a tuning-table hit, bsj_plan_autotune or
+    // bsj_plan_set_chunk.
+    int variant = 0;
+    int total_chunks[kNumChunkSizes] = {};
     int gather_grid = 1;
     int sort_cap = 0;
     HeapCfg heap{0, 1, 16, 1};   // k_heap configuration (ICH/PMS beams)
     bool has_v1 = false, has_zero = false, has_gpu = false, has_compat = false;
-    int step_grid = 1;
     // beam groups: contiguous beam ranges run as independent graph branches, so one
     // group's select overlaps the others' expansion
     struct Group {
-        StepArgs args;
-        int maxN = 0, nq_mask = 0, step_grid = 1, gather_grid = 1;
+        StepArgs args;   // chunk fields are filled per chunk size by group_args()
+        int maxN = 0, nq_mask = 0, gather_grid = 1;
+        int rule_var = 1;  // chunk size (index into kChunkSizes) of the default rule
+        int step_grid[kNumChunkSizes] = {};
         bool has_v1 = false, has_gpu = false, has_compat = false;
     };
     std::vector<Group> groups;
@@ -68,7 +75,7 @@ struct bsj_plan {
     std::vector<SegDesc> segs;
     std::vector<SegState> init;
     std::vector<int32_t> prefix;
-    std::vector<int32_t> cprefix;
+    std::vector<int32_t> cprefix[kNumChunkSizes];  // per chunk size: prefix sums of ceil(K/chunk)
     std::vector<int32_t> group_init;
     std::vector<int32_t> seg_group;
     // segment i holds the caller's beam perm[i]: beams are laid out longest search first so
@@ -82,13 +89,13 @@ struct bsj_plan {
     SegState* d_state = nullptr;
     SegState* d_state_init = nullptr;
     int32_t* d_prefix = nullptr;
-    int32_t* d_cprefix = nullptr;
+    int32_t* d_cprefix = nullptr;   // kNumChunkSizes arrays of nseg+1
     int32_t* d_group = nullptr;
     int32_t* d_group_init = nullptr;
     size_t beam_bytes = 0, slot_bytes = 0;
     StepArgs args{};
-    // graphs: [0] plain, [1] with timing events recorded around each launch
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // graphs per chunk variant: [0] plain, [1] with timing events recorded around each launch
+    cudaGraphExec_t graph[kNumChunkSizes + 1][2] = {};
     // timing
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -164,6 +171,58 @@ bsj_status validate_instance(bsj_context* ctx, const bsj_instance& in)
 
 std::string shape_key(int ninst, const bsj_instance* insts, int nbeams, const bsj_beam* beams);
 
+// ---- k_step chunk size: tuning table and default rule ----
+// The table maps (device, plan shape) to the chunk size bsj_plan_autotune measured fastest;
+// it is shared by every context and server of the process, so a shape tuned once (e.g. by
+// a warm-up batch) is reused by later plans of that shape on any context.
+std::mutex g_tune_mu;
+std::vector<std::pair<std::string, int>> g_tuned;  // most recent last
+constexpr size_t kTuneTable = 1024;
+
+std::string tune_key(const bsj_context* ctx, const std::string& shape)
+{
+    return std::to_string(ctx->device) + "#" + shape;
+}
+
+int tuned_chunk(const bsj_context* ctx, const std::string& shape)
+{
+    const std::string k = tune_key(ctx, shape);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto& e : g_tuned)
+        if (e.first == k) return e.second;
+    return -1;
+}
+
+void remember_chunk(const bsj_context* ctx, const std::string& shape, int v)
+{
+    const std::string k = tune_key(ctx, shape);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto& e : g_tuned)
+        if (e.first == k) { e.second = v; return; }
+    if (g_tuned.size() >= kTuneTable) g_tuned.erase(g_tuned.begin());
+    g_tuned.push_back({k, v});
+}
+
+int chunk_var_of(int chunk)
+{
+    for (int v = 0; v < kNumChunkSizes; v++)
+        if (kChunkSizes[v] == chunk) return v;
+    return -1;
+}
+
+// Default rule for one beam group: `ranks` = survivors per level of the whole plan (all
+// groups run at once), `nq` = ceil(n/32) class holding most of the group's survivors.
+// Measured on GB300 (bench.py --chunk-sweep, gpu-v2, 18 shapes from 10x5 K=256 to 100x20
+// 8x4096, the rule picks the fastest size on all): up to 8 192 survivors per level the
+// level is narrow and 8 per CTA spreads it over the most SMs (3-30 % faster than 16), except
+// for n > 64 at 4 096 and more, where per-CTA set-up dominates and 32 wins; wider levels
+// amortise the set-up with 32, except 33 <= n <= 64, where 16 keeps more warps resident.
+int rule_chunk_var(int64_t ranks, int nq)
+{
+    if (ranks <= 8192) return chunk_var_of((nq == 4 && ranks >= 4096) ? 32 : 8);
+    return chunk_var_of(nq == 2 ? 16 : 32);
+}
+
 // With `bytes_only` non-null, computes the plan's device footprint into it and allocates
 // nothing (*out is left untouched).
 bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, int nbeams,
@@ -221,7 +280,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
            off_aux = 0, off_seq = 0, off_pos = 0;
     int sb_max = 16, max_n = 1;
     p->prefix.push_back(0);
-    p->cprefix.push_back(0);
+    for (int v = 0; v < kNumChunkSizes; v++) p->cprefix[v].push_back(0);
     for (int si = 0; si < nbeams; si++) {
         const int b = p->perm[si];
         const bsj_beam& bm = beams[b];
@@ -243,9 +302,10 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         d.op_off = inst_off[bm.instance];
         d.nq = nq_class(d.n);
         p->nq_mask |= 1 << d.nq;
-        const int nch = (d.K + kChunk - 1) / kChunk;
+        // per-chunk key counts for the smallest chunk size (the most chunks), key regions
+        // for the largest (the most padding)
         d.kcnt_off = (int32_t)off_kcnt;
-        off_kcnt += nch;
+        off_kcnt += (d.K + kMinChunk - 1) / kMinChunk;
         const size_t K = (size_t)d.K, n = (size_t)d.n, N = (size_t)d.N;
         const bool gpu = d.mode <= BSJ_MODE_CLEAN;
         const int nbuf = (d.mode == BSJ_MODE_V1) ? 1 : 2;
@@ -255,7 +315,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         d.slot_off = (int64_t)off_slot;
         if (d.mode == BSJ_MODE_V1) off_slot += align_up(K * n * d.sbytes, 256);
         d.key_off = (int64_t)off_keys;
-        if (gpu) off_keys += align_up((size_t)nch * kChunk * n, 32);
+        if (gpu) off_keys += align_up((size_t)((d.K + kMaxChunk - 1) / kMaxChunk) * kMaxChunk * n, 32);
         d.sel_off = (int64_t)off_sel;
         off_sel += align_up(K, 64);
         d.mask_off = (int64_t)off_mask;
@@ -273,7 +333,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         }
         p->segs.push_back(d);
         p->prefix.push_back(p->prefix.back() + d.K);
-        p->cprefix.push_back(p->cprefix.back() + nch);
+        for (int v = 0; v < kNumChunkSizes; v++)
+            p->cprefix[v].push_back(p->cprefix[v].back() + (d.K + kChunkSizes[v] - 1) / kChunkSizes[v]);
         sb_max = std::max(sb_max, d.sbytes);
         max_n = std::max(max_n, d.n);
         p->maxN = std::max(p->maxN, d.N);
@@ -299,7 +360,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         p->seg_group.push_back(gid[b]);
     }
     p->total_ranks = p->prefix.back();
-    p->total_chunks = p->cprefix.back();
+    for (int v = 0; v < kNumChunkSizes; v++) p->total_chunks[v] = p->cprefix[v].back();
     if (p->has_gpu) {
         int sc = 1;
         while (sc < p->sort_cap) sc <<= 1;
@@ -323,7 +384,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     const size_t o_state = take(sizeof(SegState) * nbeams);
     const size_t o_state_init = take(sizeof(SegState) * nbeams);
     const size_t o_prefix = take(sizeof(int32_t) * (nbeams + 1));
-    const size_t o_cprefix = take(sizeof(int32_t) * (nbeams + 1));
+    const size_t o_cprefix = take(sizeof(int32_t) * (nbeams + 1) * kNumChunkSizes);
     const size_t o_kcnt = take(sizeof(int32_t) * off_kcnt);
     const size_t o_group = take(sizeof(int32_t) * p->ngroups);
     const size_t o_group_init = take(sizeof(int32_t) * p->ngroups);
@@ -369,12 +430,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.total_ranks = p->total_ranks;
     a.seg_lo = 0;
     a.seg_hi = nbeams;
-    a.chunk_lo = 0;
-    a.chunk_hi = p->total_chunks;
     a.rank_lo = 0;
     a.rank_hi = p->total_ranks;
-    a.chunk_prefix = p->d_cprefix;
-    a.total_chunks = p->total_chunks;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
     a.sb_max = sb_max;
     a.max_n = max_n;
@@ -398,7 +455,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_segs, p->segs.data(), sizeof(SegDesc) * nbeams, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_state_init, p->init.data(), sizeof(SegState) * nbeams, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_prefix, p->prefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_cprefix, p->cprefix.data(), sizeof(int32_t) * (nbeams + 1), cudaMemcpyHostToDevice, st);
+    for (int v = 0; v < kNumChunkSizes && e == cudaSuccess; v++)
+        e = cudaMemcpyAsync(p->d_cprefix + (size_t)v * (nbeams + 1), p->cprefix[v].data(), sizeof(int32_t) * (nbeams + 1),
+                            cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_group_init, p->group_init.data(), sizeof(int32_t) * p->ngroups, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_ops, ops.data(), sizeof(uint32_t) * ops.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = launch_noise_table(reinterpret_cast<float*>(base + o_noise),
@@ -416,9 +475,6 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         delete p;
         return cuda_fail(ctx, e, "configure kernels");
     }
-    // warps of k_step: one per rank, 8 per CTA, up to 8 CTAs per SM resident
-    // k_step: one CTA per chunk of kChunk ranks
-    p->step_grid = std::max(1, std::min(p->total_chunks, 65535));
     int want = (p->total_ranks + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
     p->gather_grid = std::max(1, std::min(want, ctx->sm_count * 8));
     // beam groups, balanced by work (K * levels); BSJ_MAX_BEAM_GROUPS in the environment
@@ -449,8 +505,6 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             gr.args = p->args;
             gr.args.seg_lo = lo;
             gr.args.seg_hi = hi;
-            gr.args.chunk_lo = p->cprefix[lo];
-            gr.args.chunk_hi = p->cprefix[hi];
             gr.args.rank_lo = p->prefix[lo];
             gr.args.rank_hi = p->prefix[hi];
             for (int b = lo; b < hi; b++) {
@@ -460,7 +514,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
                 if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
                 if (d.mode <= BSJ_MODE_CLEAN) gr.has_gpu = true; else gr.has_compat = true;
             }
-            gr.step_grid = std::max(1, std::min(p->cprefix[hi] - p->cprefix[lo], 65535));
+            // k_step: one CTA per chunk
+            for (int v = 0; v < kNumChunkSizes; v++)
+                gr.step_grid[v] = std::max(1, std::min(p->cprefix[v][hi] - p->cprefix[v][lo], 65535));
             const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
             gr.gather_grid = std::max(1, std::min(wr, ctx->sm_count * 8));
             p->groups.push_back(gr);
@@ -469,8 +525,39 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
         for (int g = 0; g < (int)p->groups.size(); g++) cudaEventCreateWithFlags(&p->join[g], cudaEventDisableTiming);
     }
+    // chunk sizes: the default rule per group; the variant tuning found for this shape on
+    // this device, else the rule
+    for (auto& gr : p->groups) {
+        int64_t per_nq[5] = {0, 0, 0, 0, 0};
+        for (int b = gr.args.seg_lo; b < gr.args.seg_hi; b++) per_nq[p->segs[b].nq] += p->segs[b].K;
+        const int nq = per_nq[4] > per_nq[2] && per_nq[4] > per_nq[1] ? 4 : (per_nq[2] > per_nq[1] ? 2 : 1);
+        gr.rule_var = rule_chunk_var(p->total_ranks, nq);
+    }
+    {
+        const int v = tuned_chunk(ctx, p->shape);
+        p->variant = v >= 0 ? v : 0;
+    }
     *out = p;
     return BSJ_OK;
+}
+
+// Chunk size (index into kChunkSizes) group `gr` runs with under the plan's variant.
+int group_var(const bsj_plan* p, const bsj_plan::Group& gr)
+{
+    return p->variant == 0 ? gr.rule_var : p->variant - 1;
+}
+
+// The launch arguments of group `gr` (whole plan: nullptr) for chunk size kChunkSizes[v].
+StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
+{
+    StepArgs a = gr ? gr->args : p->args;
+    const int lo = gr ? a.seg_lo : 0, hi = gr ? a.seg_hi : p->nseg;
+    a.chunk = kChunkSizes[v];
+    a.chunk_prefix = p->d_cprefix + (size_t)v * (p->nseg + 1);
+    a.chunk_lo = p->cprefix[v][lo];
+    a.chunk_hi = p->cprefix[v][hi];
+    a.total_chunks = p->total_chunks[v];
+    return a;
 }
 
 cudaEvent_t* next_events(bsj_plan* p, int cls)
@@ -490,7 +577,7 @@ cudaEvent_t* next_events(bsj_plan* p, int cls)
 // timing events become event-record nodes of the graph).
 cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
 {
-    const StepArgs& a = p->args;
+    const StepArgs a = group_args(p, nullptr, chunk_var_of(kDefaultChunk));  // finalize: chunk unused
     cudaError_t e;
     p->launches = 0;
     p->events_used = 0;
@@ -533,8 +620,10 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
             p->launches++;
             return rec(ev[1]);
         };
-        const StepArgs& ga = gr.args;
-        cudaError_t r = timed_g(0, [&] { return launch_step(ga, -1, gr.step_grid, gr.nq_mask, gs); });
+        const int cv = group_var(p, gr);
+        const StepArgs ga = group_args(p, &gr, cv);
+        const int step_grid = gr.step_grid[cv];
+        cudaError_t r = timed_g(0, [&] { return launch_step(ga, -1, step_grid, gr.nq_mask, gs); });
         if (r != cudaSuccess) return r;
         for (int lv = 0; lv < gr.maxN; lv++) {
             if (gr.has_gpu) {
@@ -550,7 +639,7 @@ cudaError_t enqueue_run(bsj_plan* p, cudaStream_t s, bool capturing)
                     r = timed_g(3, [&] { return launch_gather_v1(ga, lv, gr.gather_grid, gs); });
                     if (r != cudaSuccess) return r;
                 }
-                r = timed_g(0, [&] { return launch_step(ga, lv, gr.step_grid, gr.nq_mask, gs); });
+                r = timed_g(0, [&] { return launch_step(ga, lv, step_grid, gr.nq_mask, gs); });
                 if (r != cudaSuccess) return r;
             }
         }
@@ -775,7 +864,8 @@ bsj_status bsj_plan_run(bsj_plan* p, void* stream)
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     p->last_stream = s;
     const int gi = p->timing ? 1 : 0;
-    if (!p->graph[gi]) {
+    cudaGraphExec_t& graph = p->graph[p->variant][gi];
+    if (!graph) {
         // capture once on the context's stream, replay on any stream
         cudaStream_t cap = ctx->stream;
         cudaGraph_t g = nullptr;
@@ -784,11 +874,11 @@ bsj_status bsj_plan_run(bsj_plan* p, void* stream)
         cudaError_t e2 = cudaStreamEndCapture(cap, &g);
         if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ctx, e, "plan capture"); }
         if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&p->graph[gi], g, 0);
+        e = cudaGraphInstantiate(&graph, g, 0);
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) { p->graph[gi] = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+        if (e != cudaSuccess) { graph = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
     }
-    BSJ_CUDA(ctx, cudaGraphLaunch(p->graph[gi], s));
+    BSJ_CUDA(ctx, cudaGraphLaunch(graph, s));
     return BSJ_OK;
 }
 
@@ -829,8 +919,9 @@ void bsj_plan_destroy(bsj_plan* p)
 {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
-    for (cudaGraphExec_t g : p->graph)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto& gv : p->graph)
+        for (cudaGraphExec_t g : gv)
+            if (g) cudaGraphExecDestroy(g);
     if (p->fork) cudaEventDestroy(p->fork);
     for (cudaEvent_t ev : p->join)
         if (ev) cudaEventDestroy(ev);
@@ -908,6 +999,78 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan* p, float* ms, int64_t* launches, i
     return BSJ_OK;
 }
 
+bsj_status bsj_plan_set_chunk(bsj_plan* p, int32_t chunk)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    if (chunk == 0) { p->variant = 0; return BSJ_OK; }
+    const int v = chunk_var_of(chunk);
+    if (v < 0) return fail(p->ctx, BSJ_ERR_INVALID, "chunk must be 0 (default rule), 8, 16 or 32");
+    p->variant = 1 + v;
+    return BSJ_OK;
+}
+
+int32_t bsj_plan_chunk(const bsj_plan* p) { return (p && p->variant > 0) ? kChunkSizes[p->variant - 1] : 0; }
+
+bsj_status bsj_plan_autotune(bsj_plan* p, void* stream, int32_t repeats, int32_t* chunk, float* ms)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    bsj_context* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    if (repeats < 1) repeats = 1;
+    // a uniform size that the rule already gives every group is not timed twice
+    int rule_uniform = -1;
+    for (const auto& gr : p->groups) {
+        if (rule_uniform == -1) rule_uniform = gr.rule_var;
+        else if (rule_uniform != gr.rule_var) rule_uniform = -2;
+    }
+    const bool timing = p->timing;
+    p->timing = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bsj_status st = BSJ_OK;
+    cudaError_t e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    if (e != cudaSuccess) st = cuda_fail(ctx, e, "autotune events");
+    float best = 0.f;
+    int bv = -1;
+    for (int v = 0; v <= kNumChunkSizes && st == BSJ_OK; v++) {
+        if (ms) ms[v] = -1.f;
+        if (v > 0 && v - 1 == rule_uniform) {
+            if (ms) ms[v] = ms[0];
+            continue;
+        }
+        p->variant = v;
+        st = bsj_plan_run(p, s);  // captures this variant's graph; untimed warm-up
+        if (st != BSJ_OK) break;
+        e = cudaEventRecord(ev[0], s);
+        for (int r = 0; r < repeats && st == BSJ_OK && e == cudaSuccess; r++) st = bsj_plan_run(p, s);
+        if (st != BSJ_OK) break;
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+        if (e != cudaSuccess) { st = cuda_fail(ctx, e, "autotune timing"); break; }
+        t /= (float)repeats;
+        if (ms) ms[v] = t;
+        if (bv < 0 || t < best) { best = t; bv = v; }
+    }
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    p->timing = timing;
+    if (st != BSJ_OK) { p->variant = 0; return st; }
+    p->variant = bv;
+    remember_chunk(ctx, p->shape, bv);
+    if (chunk) *chunk = bsj_plan_chunk(p);
+    return BSJ_OK;
+}
+
+bsj_status bsj_set_autotune(bsj_context* ctx, int32_t enable)
+{
+    if (!ctx) return BSJ_ERR_INVALID;
+    ctx->autotune = enable != 0;
+    return BSJ_OK;
+}
+
 bsj_status bsj_solve_batch(bsj_context* ctx, int num_instances, const bsj_instance* instances,
                            int num_beams, const bsj_beam* beams, bsj_result* results, void* stream)
 {
@@ -948,10 +1111,18 @@ bsj_status solve_batch_impl(bsj_context* ctx, int num_instances, const bsj_insta
         if (s != BSJ_OK) bsj_plan_destroy(p);
     }
     if (s != BSJ_OK) return s;
-    // first call of this shape: eager launches (capturing a graph pays off on reuse only)
-    p->last_stream = st;
-    cudaError_t e = enqueue_run(p, st, false);
-    if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
+    if (ctx->autotune && tuned_chunk(ctx, key) < 0) {
+        // tune the new shape; every candidate run computes the same results
+        s = bsj_plan_autotune(p, st, 1, nullptr, nullptr);
+        if (s != BSJ_OK) { bsj_plan_destroy(p); return s; }
+        s = bsj_plan_run(p, st);
+        if (s != BSJ_OK) { bsj_plan_destroy(p); return s; }
+    } else {
+        // first call of this shape: eager launches (capturing a graph pays off on reuse only)
+        p->last_stream = st;
+        cudaError_t e = enqueue_run(p, st, false);
+        if (e != cudaSuccess) { bsj_plan_destroy(p); return cuda_fail(ctx, e, "solve"); }
+    }
     s = bsj_plan_results(p, results);
     if (s == BSJ_OK && rand_out) s = plan_get_rand(p, rand_out);
     if (s != BSJ_OK) { bsj_plan_destroy(p); return s; }

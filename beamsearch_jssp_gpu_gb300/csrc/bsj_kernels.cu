@@ -357,13 +357,13 @@ __device__ void expand_compat(uint8_t* sb, const Lay& L, const SegDesc& d, const
 }
 
 // ------------------------------------------------------------------------------------
-// k_step: materialise level s+1 and expand it.  Work unit: a chunk of kChunk consecutive
-// ranks of one beam per CTA (kRanksPerWarp per warp).  Each warp first fetches the
+// k_step: materialise level s+1 and expand it.  Work unit: a chunk of CH consecutive
+// ranks of one beam per CTA (CH / 8 per warp; CH = a.chunk, chosen per plan).  Each warp first fetches the
 // selection entries of its ranks, then starts asynchronous copies of all their source
 // snapshots into shared memory, then materialises and expands them one after the other,
 // so the copies of later ranks overlap the work on earlier ones.  NQ = ceil(n/32).
 // ------------------------------------------------------------------------------------
-template <int NQ>
+template <int NQ, int CH>
 #ifndef BSJ_STEP_MIN_BLOCKS
 #define BSJ_STEP_MIN_BLOCKS 4
 #endif
@@ -375,9 +375,10 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32,
                                   NQ == 4 ? 3 : NQ == 2 ? BSJ_STEP_MIN_BLOCKS_NQ2 : BSJ_STEP_MIN_BLOCKS)
 k_step(StepArgs a, int s)
 {
+    constexpr int kRanksPerWarp = CH / kWarpsPerStepCta;
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ float s_noise[1000];
-    __shared__ int s_nv[kChunk], s_pre[kChunk], s_kcnt, s_P;
+    __shared__ int s_nv[CH], s_pre[CH], s_kcnt, s_P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint8_t* wbuf = smem + (size_t)warp * (kRanksPerWarp + 1) * a.sb_max;
     uint8_t* cb = wbuf + (size_t)kRanksPerWarp * a.sb_max;
@@ -395,13 +396,13 @@ k_step(StepArgs a, int s)
         SegState& st = a.st[seg];
         const int q = chunk - __ldg(a.chunk_prefix + seg);
         if (threadIdx.x == 0) s_P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
-        if (threadIdx.x < kChunk) s_nv[threadIdx.x] = 0;
+        if (threadIdx.x < CH) s_nv[threadIdx.x] = 0;
         __syncthreads();
         const int P = s_P;
         const Lay L(d);
         const int mode = d.mode;
         const bool compat = (mode == MODE_ICH || mode == MODE_PMS);
-        const int r0 = q * kChunk + warp;
+        const int r0 = q * CH + warp;
         uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
         const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
         if (mode == MODE_V1) childbuf = a.beam_pool + d.beam_off[0];
@@ -432,7 +433,7 @@ k_step(StepArgs a, int s)
         cp_async_wait_all();
         __syncwarp();
 
-        unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * kChunk * L.n;
+        unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * CH * L.n;
         const int nst = L.n;  // staged keys per rank
         uint32_t* hrow = a.hist + d.hist_off + (int64_t)(s < 0 ? 0 : s) * d.K;
 #pragma unroll 1
@@ -474,7 +475,7 @@ k_step(StepArgs a, int s)
             __syncwarp();
             if (compat) expand_compat<NQ>(sb, L, d, a, r, lane);
             else {
-                const int rl = r - q * kChunk;
+                const int rl = r - q * CH;
                 expand_gpu<NQ>(sb, cb, L, d, st, a, r, s + 1, lane, kstage + (size_t)rl * nst, &s_nv[rl], s_noise);
             }
         }
@@ -482,18 +483,18 @@ k_step(StepArgs a, int s)
         if (!compat) {
             // rank-ordered prefix of the staged counts, then coalesced copy-out
             if (warp == 0) {
-                const int v = lane < kChunk ? s_nv[lane] : 0;
+                const int v = lane < CH ? s_nv[lane] : 0;
                 int x = v;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const int y = __shfl_up_sync(FULL_MASK, x, o);
                     if (lane >= o) x += y;
                 }
-                if (lane < kChunk) s_pre[lane] = x - v;
+                if (lane < CH) s_pre[lane] = x - v;
                 if (lane == 31) s_kcnt = x;
             }
             __syncthreads();
-            for (int rl = warp; rl < kChunk; rl += kWarpsPerStepCta) {
+            for (int rl = warp; rl < CH; rl += kWarpsPerStepCta) {
                 const int cntk = s_nv[rl];
                 const int dst0 = s_pre[rl];
                 for (int i = lane; i < cntk; i += 32) kdst[dst0 + i] = kstage[(size_t)rl * nst + i];
@@ -1507,7 +1508,7 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     SegState& st = a.st[seg];
     // candidate counts of the level's chunks -> prefix, V (up to 2 chunks per thread)
     constexpr int CPT = (kMaxChunks + kSelectThreads - 1) / kSelectThreads;
-    const int nch = (d.K + kChunk - 1) / kChunk;
+    const int nch = (d.K + a.chunk - 1) / a.chunk;
     const int c0 = threadIdx.x * CPT;
     int cv[CPT], v = 0;
 #pragma unroll
@@ -1534,7 +1535,7 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     ks.base = a.keys + d.key_off;
     ks.cpref = s_cpref;
     ks.nch = nch;
-    ks.cap = kChunk * d.n;
+    ks.cap = a.chunk * d.n;
     select_gpu(d, st, a, V, ks, smem);
 }
 
@@ -2073,9 +2074,26 @@ __global__ void k_finalize(StepArgs a)
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
-size_t step_smem_bytes(int sb_max, int max_n)
+size_t step_smem_bytes(int sb_max, int max_n, int chunk)
 {
-    return (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * sb_max + (size_t)kChunk * max_n * 8;
+    return (size_t)kWarpsPerStepCta * (chunk / kWarpsPerStepCta + 1) * sb_max + (size_t)chunk * max_n * 8;
+}
+
+// every k_step instantiation: NQ in {1, 2, 4} x chunk in kChunkSizes
+template <typename F>
+static cudaError_t for_each_step(F&& f)
+{
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = f(k_step<1, 8>, 8);
+    if (e == cudaSuccess) e = f(k_step<2, 8>, 8);
+    if (e == cudaSuccess) e = f(k_step<4, 8>, 8);
+    if (e == cudaSuccess) e = f(k_step<1, 16>, 16);
+    if (e == cudaSuccess) e = f(k_step<2, 16>, 16);
+    if (e == cudaSuccess) e = f(k_step<4, 16>, 16);
+    if (e == cudaSuccess) e = f(k_step<1, 32>, 32);
+    if (e == cudaSuccess) e = f(k_step<2, 32>, 32);
+    if (e == cudaSuccess) e = f(k_step<4, 32>, 32);
+    return e;
 }
 
 int nq_class(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
@@ -2087,9 +2105,8 @@ static cudaError_t set_carveout()
     const int c = cudaSharedmemCarveoutMaxShared;
     cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<1>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<2>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step<4>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess)
+        e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gather_v1, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     return e;
@@ -2116,9 +2133,8 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     cudaError_t e = set_carveout();
     if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
     if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
-    if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
-    if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
-    if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess)
+        e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     return e;
 }
 
@@ -2126,9 +2142,8 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
 {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e == cudaSuccess) e = raise_smem(k_step<1>, step_smem_bytes(sb_max, max_n));
-    if (e == cudaSuccess) e = raise_smem(k_step<2>, step_smem_bytes(sb_max, max_n));
-    if (e == cudaSuccess) e = raise_smem(k_step<4>, step_smem_bytes(sb_max, max_n));
+    if (e == cudaSuccess)
+        e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     return e;
 }
 
@@ -2157,15 +2172,26 @@ static cudaError_t launch_kernel(void (*kern)(KArgs...), int grid, int block, si
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
+template <int CH>
+static cudaError_t launch_step_ch(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
-    const size_t sm = step_smem_bytes(a.sb_max, a.max_n);
+    const size_t sm = step_smem_bytes(a.sb_max, a.max_n, CH);
     const int block = kWarpsPerStepCta * 32;
     cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess && (nq_mask & 2)) e = launch_kernel(k_step<1>, grid, block, sm, stream, s >= 0, a, s);
-    if (e == cudaSuccess && (nq_mask & 4)) e = launch_kernel(k_step<2>, grid, block, sm, stream, s >= 0, a, s);
-    if (e == cudaSuccess && (nq_mask & 16)) e = launch_kernel(k_step<4>, grid, block, sm, stream, s >= 0, a, s);
+    if (e == cudaSuccess && (nq_mask & 2)) e = launch_kernel(k_step<1, CH>, grid, block, sm, stream, s >= 0, a, s);
+    if (e == cudaSuccess && (nq_mask & 4)) e = launch_kernel(k_step<2, CH>, grid, block, sm, stream, s >= 0, a, s);
+    if (e == cudaSuccess && (nq_mask & 16)) e = launch_kernel(k_step<4, CH>, grid, block, sm, stream, s >= 0, a, s);
     return e;
+}
+
+cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
+{
+    switch (a.chunk) {
+    case 8: return launch_step_ch<8>(a, s, grid, nq_mask, stream);
+    case 16: return launch_step_ch<16>(a, s, grid, nq_mask, stream);
+    case 32: return launch_step_ch<32>(a, s, grid, nq_mask, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream)

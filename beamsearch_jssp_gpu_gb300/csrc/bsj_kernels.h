@@ -13,7 +13,7 @@ struct StepArgs {
     const SegDesc* segs;
     SegState* st;
     const int32_t* rank_prefix;   // [nseg+1] prefix sums of K (flattened rank space)
-    const int32_t* chunk_prefix;  // [nseg+1] prefix sums of ceil(K/kChunk)
+    const int32_t* chunk_prefix;  // [nseg+1] prefix sums of ceil(K/chunk)
     int32_t* kcnt;                // candidate keys per chunk of the current level
     int32_t nseg;
     int32_t total_ranks;
@@ -25,7 +25,7 @@ struct StepArgs {
     int32_t seg_lo, seg_hi;
     int32_t chunk_lo, chunk_hi;
     int32_t rank_lo, rank_hi;
-    int32_t pad0;
+    int32_t chunk;                // ranks per k_step CTA (one of kChunkSizes)
     uint8_t* beam_pool;
     uint8_t* slot_pool;
     unsigned long long* keys;
@@ -48,15 +48,15 @@ struct HeapCfg {
 };
 
 // Grid / shared-memory sizing helpers.
-size_t step_smem_bytes(int sb_max, int max_n);
+size_t step_smem_bytes(int sb_max, int max_n, int chunk);
 size_t select_smem_bytes(int sort_cap);
 size_t heap_smem_bytes(const HeapCfg& c);
 // Largest chunk in [1, kHeapMaxChunk] whose k_heap shared memory fits `budget`; 0 if none.
 int heap_pick_chunk(HeapCfg c, size_t budget);
 
 // Launchers (asynchronous on `stream`).
-// k_step is instantiated per NQ = ceil(n/32) in {1, 2, 4}; nq_mask has bit NQ set for
-// each class present in the batch (one launch per class).
+// k_step is instantiated per NQ = ceil(n/32) in {1, 2, 4} and chunk size (a.chunk);
+// nq_mask has bit NQ set for each class present in the batch (one launch per class).
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream);
 int nq_class(int n);
 cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t stream);

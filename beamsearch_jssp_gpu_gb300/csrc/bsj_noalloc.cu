@@ -123,7 +123,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     d.op_off = 0;
     d.nq = nq_class(n);
     d.kcnt_off = 0;
-    const int nch = (beam_width + kChunk - 1) / kChunk;
+    const int nch = (beam_width + kDefaultChunk - 1) / kDefaultChunk;
     const size_t K = (size_t)beam_width, N = (size_t)d.N;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return at; };
@@ -135,7 +135,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     const size_t o_group = take(sizeof(int32_t));
     const size_t o_ops = take(N * sizeof(uint32_t));
     const size_t o_beam = take(2 * align_up(K * d.sbytes, 256));
-    const size_t o_keys = take((size_t)nch * kChunk * n * 8);
+    const size_t o_keys = take((size_t)nch * kDefaultChunk * n * 8);
     const size_t o_sel = take(K * 4);
     const size_t o_mask = take(K * d.words * 4);
     const size_t o_hist = take(N * K * 4);
@@ -175,6 +175,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     a.chunk_hi = nch;
     a.rank_lo = 0;
     a.rank_hi = beam_width;
+    a.chunk = kDefaultChunk;
     a.chunk_prefix = reinterpret_cast<const int32_t*>(base + o_cprefix);
     a.total_chunks = nch;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);

@@ -141,6 +141,10 @@ class Context:
     def plan(self, instances: Sequence, beams: Sequence[BeamSpec]) -> "Plan":
         return Plan(self, instances, beams)
 
+    def set_autotune(self, on: bool):
+        """Tune every new batch shape on its first solve (bsj_set_autotune)."""
+        self._check(self.lib.bsj_set_autotune(self.h, 1 if on else 0))
+
     def estimate(self, instances: Sequence, beams: Sequence[BeamSpec]) -> int:
         """Device bytes a plan of this batch would hold (bsj_plan_estimate)."""
         ia = _InstanceArrays(instances)
@@ -209,6 +213,26 @@ class Plan:
 
     def set_timing(self, on: bool):
         self.ctx._check(self.lib.bsj_plan_set_timing(self.h, 1 if on else 0))
+
+    def autotune(self, repeats: int = 2, stream: int = 0) -> dict:
+        """Time every k_step chunk candidate on this plan and keep the fastest
+        (bsj_plan_autotune).  Returns {"chunk": choice, "ms": {candidate: ms per run}},
+        candidates 0 (the default rule), 8, 16, 32."""
+        ch = ctypes.c_int32()
+        ms = (ctypes.c_float * len(nat.CHUNK_CANDIDATES))()
+        self.ctx._check(self.lib.bsj_plan_autotune(self.h, ctypes.c_void_p(stream) if stream else None,
+                                                   int(repeats), ctypes.byref(ch), ms))
+        return {"chunk": int(ch.value), "ms": {c: float(ms[i]) for i, c in enumerate(nat.CHUNK_CANDIDATES)}}
+
+    @property
+    def chunk(self) -> int:
+        """Survivors per k_step thread block: 8, 16 or 32 for every beam group, or 0 for
+        the default rule's per-group sizes."""
+        return int(self.lib.bsj_plan_chunk(self.h))
+
+    @chunk.setter
+    def chunk(self, value: int):
+        self.ctx._check(self.lib.bsj_plan_set_chunk(self.h, int(value)))
 
     KERNELS = ("k_step", "k_select", "k_heap", "k_gather_v1", "k_finalize")
 

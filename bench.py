@@ -20,7 +20,8 @@ Also on the JSON line (rank 0; --no-extras skips them):
              serial bounded heap per beam), candidates/s and makespans;
   "batched"  256 synthetic instances of uneven size (n in {10..100}, m in {5..20},
              K in {256..4096}) in one bsj_solve_batch, solves/s against the same
-             instances solved one call at a time (the plain path), makespans compared;
+             instances solved one call at a time (the plain path), makespans compared; the
+             batch's k_step chunk sizes are autotuned on its first call (untimed);
   "serving"  400 requests with Poisson arrivals through bsj_server (continuous
              batching) at 150/s (sustained) and 1000/s (overload), solves/s and p50/p99
              latency per rate against the plain path on the same requests, results
@@ -240,6 +241,8 @@ def gpu_arm(args) -> int:
 
     with torch.cuda.stream(stream):
         plan.set_timing(False)
+        # autotuner: k_step chunk size for this shape (untimed; results do not depend on it)
+        tune = plan.autotune(repeats=1, stream=sh)
         for _ in range(args.warmup):
             plan.run(sh)
         torch.cuda.synchronize()
@@ -322,6 +325,8 @@ def gpu_arm(args) -> int:
                 "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clk,
                 "select_fallback_levels": stats["select_fallbacks"],
+                "autotune": {"chunk": tune["chunk"], "ms_per_candidate": {str(k): round(v, 3) for k, v in
+                                                                          tune["ms"].items()}},
                 "makespans": [r["makespan"] for r in res], **extras}
         print(json.dumps(line), flush=True)
     plan.close()
@@ -377,7 +382,9 @@ def batched_stream(ctx, count: int = 256, seed: int = 1) -> dict:
         K = rng.choice([256, 512, 1024, 4096])
         insts.append(synthetic_instance(n, m, 10000 + i))
         beams.append(BeamSpec("v2", K, 500000, rng.randrange(1 << 30), i, -1))
-    ctx.solve_batch(insts, beams)                      # builds and caches the batch plan
+    ctx.set_autotune(True)
+    ctx.solve_batch(insts, beams)                      # builds, tunes and caches the batch plan
+    ctx.set_autotune(False)
     t0 = time.perf_counter()
     out = ctx.solve_batch(insts, beams)
     t_batch = time.perf_counter() - t0
@@ -503,6 +510,33 @@ def k_sweep(args) -> int:
     return 0
 
 
+def chunk_sweep(args) -> int:
+    """Autotuner data: per shape (n, m, K, beams; gpu-v2 mode) the ms per search of each
+    k_step chunk candidate (0 = the default rule; 8, 16, 32 survivors per thread block),
+    from bsj_plan_autotune.  One JSON line per shape."""
+    import torch
+
+    from beamsearch_jssp_gpu_gb300 import BeamSpec, Context, synthetic_instance
+
+    shapes = [(10, 5, 256, 1), (15, 15, 256, 1), (20, 15, 256, 1), (20, 15, 1024, 1), (20, 15, 1024, 8),
+              (20, 15, 4096, 1), (20, 15, 4096, 8), (30, 20, 1024, 1), (30, 20, 4096, 1), (30, 20, 4096, 8),
+              (50, 20, 256, 1), (50, 20, 1024, 1), (50, 20, 4096, 1), (50, 20, 4096, 8), (100, 20, 1024, 1),
+              (100, 20, 4096, 1), (100, 20, 4096, 8), (20, 15, 16384, 1)]
+    ctx = Context(0)
+    stream = torch.cuda.Stream()
+    for n, m, K, nb in shapes:
+        mc, du = synthetic_instance(n, m, 0)
+        plan = ctx.plan([(mc, du)], [BeamSpec("v2", K, 500000, b, 0, 0) for b in range(nb)])
+        with torch.cuda.stream(stream):
+            out = plan.autotune(repeats=max(1, args.steps), stream=stream.cuda_stream)
+        print(json.dumps({"metric": "chunk-sweep, gpu-v2", "jobs": n, "machines": m, "beam_width": K,
+                          "beams": nb, "chunk": out["chunk"],
+                          "ms": {str(c): round(v, 3) for c, v in out["ms"].items()}}), flush=True)
+        plan.close()
+    ctx.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,9 +546,13 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and served streams")
     ap.add_argument("--k-sweep", action="store_true", help="time vs beam width (20x15, gpu-v1), one line per K")
+    ap.add_argument("--chunk-sweep", action="store_true",
+                    help="ms per search of each k_step chunk size over a set of shapes (autotuner data)")
     args = ap.parse_args()
     if args.k_sweep:
         return k_sweep(args)
+    if args.chunk_sweep:
+        return chunk_sweep(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

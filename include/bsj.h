@@ -161,6 +161,32 @@ bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, double *sele
 bsj_status bsj_plan_set_timing(bsj_plan *plan, int enable);
 bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches, int count);
 
+/* ---- Autotuning (no counterpart in the reference, whose launch shape is fixed:
+   one block of n threads per parent, gpu/v1/solver.cu:186,237) ----
+   The materialise+expand kernel works on chunks of consecutive survivors of one beam per
+   thread block: 8, 16 or 32 (1, 2 or 4 per warp).  Small chunks spread a narrow level
+   over more SMs, large ones amortise per-block work; which is faster depends on n, m, K
+   and the number of beams, and results never depend on it.  Each beam group of a plan
+   (a graph branch) has its own size.  Candidates ("chunk" values): 0 = the default rule
+   (per group, from the plan's survivors per level and the group's n), 8, 16, 32 = that
+   size for every group.
+   bsj_plan_autotune runs the plan once per candidate (an untimed run that also captures
+   its graph, then `repeats` timed runs on `stream`, synchronously), keeps the fastest,
+   and records it in a process-wide table keyed by device and batch shape, so later plans
+   of the same shape (any context, the server included) start with it.  ms (may be NULL)
+   receives the mean ms per run of each candidate in the order 0, 8, 16, 32 (a uniform
+   size equal to what the rule gives every group is not run again: its entry repeats the
+   rule's); *chunk (may be NULL) the choice.  The plan's results afterwards are those of
+   a complete run.  Plans start with the tuned candidate of their shape if there is one,
+   else the rule.  bsj_plan_set_chunk selects a candidate; bsj_plan_chunk returns it.
+   bsj_set_autotune: with enable != 0, bsj_solve_batch / bsj_solve tune every batch shape
+   they have not seen on this device before its first solve (about 4 extra solves once
+   per shape). */
+bsj_status bsj_plan_autotune(bsj_plan *plan, void *stream, int32_t repeats, int32_t *chunk, float *ms);
+bsj_status bsj_plan_set_chunk(bsj_plan *plan, int32_t chunk);
+int32_t bsj_plan_chunk(const bsj_plan *plan);
+bsj_status bsj_set_autotune(bsj_context *ctx, int32_t enable);
+
 /* Instance files in the reference's text format (cpu/common/instance_parser.cpp:8-93).
    bsj_instance_resolve: `arg` as a path, else the reference's Lawrence/Taillard search
    list; BSJ_ERR_INVALID when nothing is found.  bsj_instance_read: *n, *m from the header;
