@@ -1420,6 +1420,125 @@ __device__ bool select_large(SegState& st, int R, const KeySrc& ks, uint32_t* se
     return true;
 }
 
+// ---- direct staged selection: the common case of a level that fits the staging area.
+// After the bucket threshold, the distinct scores of the keys of buckets <= T get dense
+// ranks (at most 256 of them); one stable counting pass over the staged keys, in slot
+// order, then gives every kept key its final position in (score, slot) order -- the
+// reference's stable sort order -- and survivors below R go straight to `sel`.  Warps own
+// contiguous runs of the staged keys: pass 1 walks each run tile by tile, ranking a key
+// against its tile peers (bit ballots of the digit) and the warp's running per-digit
+// counters, and writes (digit << 16 | offset) over the key's score bits; after a
+// digit-major prefix over (digit, warp), pass 2 scatters in parallel.  No compaction
+// buffer, no sort passes.  Returns false -- staged keys untouched, nothing written -- when
+// the dense tables do not fit or there are more than 256 distinct scores; the general
+// path then runs.  Taken for levels of up to kDirectMaxKeys keys. ----
+constexpr int kDirectMaxDistinct = 256;
+// Largest level (candidate keys) the direct path takes: beyond it, compacting the keys
+// first and sorting the survivors is faster (a GB300 sweep over 18 shapes: the direct
+// path wins 5-10 % up to ~4 K keys, loses from ~6 K on).
+constexpr int kDirectMaxKeys = 4096;
+
+__device__ bool select_direct(unsigned long long* stg, int V, int R, int T, int shift, uint32_t smin, uint32_t* sel,
+                              const SelSmem& S)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    DenseTables D;
+    D.occ = reinterpret_cast<uint16_t*>(S.A);
+    D.bm = reinterpret_cast<uint32_t*>(S.A + kNB / 4);
+    D.wp = D.bm + kDenseWords;
+    auto each = [&](auto fn) {
+        for (int i = tid; i < V; i += nthr) fn(stg[i]);
+    };
+    const int nd = dense_build(each, T, shift, smin, S, D);   // reads S.hist, ends synchronised
+    if (nd < 0 || nd > kDirectMaxDistinct) return false;      // the same in every thread
+    uint16_t* wh = reinterpret_cast<uint16_t*>(S.hist);       // [32][256] per-warp digit counters
+    int* dtot = reinterpret_cast<int*>(S.tot);                // [256]
+    for (int i = tid; i < 32 * 256 / 2; i += nthr) S.hist[i] = 0u;
+    __syncthreads();
+    const uint32_t lim = ((uint32_t)T + 1u) << shift;          // bucket <= T
+    const unsigned lt = (1u << lane) - 1u;
+    const int per = ((V + nwarps - 1) / nwarps + 31) & ~31;   // <= 512: offsets fit 16 bits
+    const int lo = min(V, warp * per), hi = min(V, lo + per);
+    // two tiles per step: their digits and peer sets are independent; only the counter
+    // updates run in tile order
+    auto tile = [&](int i, unsigned long long& k, int& dg, unsigned& grp) {
+        k = ~0ull;
+        dg = 0;
+        bool kept = false;
+        if (i < hi) {
+            k = stg[i];
+            const uint32_t sb = (uint32_t)(k >> 32);
+            kept = (sb - smin) < lim;
+            if (kept) dg = (int)D.rank_of(sb);
+        }
+        grp = __ballot_sync(FULL_MASK, kept);
+#pragma unroll
+        for (int bit = 0; bit < 8; bit++) {
+            const unsigned bb = __ballot_sync(FULL_MASK, (dg >> bit) & 1);
+            grp &= ((dg >> bit) & 1) ? bb : ~bb;
+        }
+        if (!kept) grp = 0u;
+    };
+    auto count = [&](int dg, unsigned grp) {
+        int base = 0;
+        if (grp) base = wh[warp * 256 + dg];
+        __syncwarp();
+        if (grp && (grp & lt) == 0u) wh[warp * 256 + dg] = (uint16_t)(base + __popc(grp));
+        __syncwarp();
+        return base + __popc(grp & lt);
+    };
+    for (int i0 = lo; i0 < hi; i0 += 64) {
+        const int ia = i0 + lane, ib = i0 + 32 + lane;
+        unsigned long long ka, kb;
+        int da, db;
+        unsigned ga, gb;
+        tile(ia, ka, da, ga);
+        tile(ib, kb, db, gb);
+        const int oa = count(da, ga);
+        const int ob = count(db, gb);
+        if (ia < hi) stg[ia] = ga ? ((unsigned long long)(((uint32_t)da << 16) | (uint32_t)oa) << 32) | (ka & 0xFFFFFFFFull) : ~0ull;
+        if (ib < hi) stg[ib] = gb ? ((unsigned long long)(((uint32_t)db << 16) | (uint32_t)ob) << 32) | (kb & 0xFFFFFFFFull) : ~0ull;
+    }
+    __syncthreads();
+    // per digit: exclusive prefix over the warps, then over the digits
+    if (tid < 256) {
+        int run = 0;
+        for (int w = 0; w < nwarps; w++) {
+            const int t = wh[w * 256 + tid];
+            wh[w * 256 + tid] = (uint16_t)run;
+            run += t;
+        }
+        dtot[tid] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int v8[8], sum = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { v8[u] = dtot[lane * 8 + u]; sum += v8[u]; }
+        int xx = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, xx, o);
+            if (lane >= o) xx += y;
+        }
+        int run = xx - sum;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { dtot[lane * 8 + u] = run; run += v8[u]; }
+    }
+    __syncthreads();
+    for (int i = tid; i < V; i += nthr) {
+        const unsigned long long x = stg[i];
+        const uint32_t h = (uint32_t)(x >> 32);
+        if (h != 0xFFFFFFFFu) {
+            const int dg = (int)(h >> 16);
+            const int pos = dtot[dg] + (int)wh[(i / per) * 256 + dg] + (int)(h & 0xFFFFu);
+            if (pos < R) sel[pos] = (uint32_t)(x & 0xFFFFFFFFull);
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
 __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int V, const KeySrc& ks,
                            uint8_t* smem)
 {
@@ -1445,45 +1564,49 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
         const uint32_t smin = (uint32_t)S.misc[1];
         const bool bucketed = count <= kLsdMax;   // survivors = the keys of buckets <= T
         __syncthreads();
-        if (bucketed) {
-            const uint32_t lim = ((uint32_t)T + 1u) << shift;  // bucket <= T
-            auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
-            count = staged ? compact_stable(get_s, V, keep, dst, kLsdMax, S)
-                           : compact_stable(get_g, V, keep, dst, kLsdMax, S);
-        } else {
-            if (tid == 0) st.select_fallbacks += 1;
-            unsigned long long pmask, prefix;
-            if (staged) radix_threshold(get_s, V, R, S, pmask, prefix);
-            else radix_threshold(get_g, V, R, S, pmask, prefix);
-            auto keep = [=](unsigned long long k) { return (k & pmask) <= prefix; };
-            if (R > kLsdMax) dst = S.stg;  // only reached unstaged (K > kLsdMax)
-            const int cap = (R > kLsdMax) ? kStageKeys : kLsdMax;
-            count = staged ? compact_stable(get_s, V, keep, dst, cap, S)
-                           : compact_stable(get_g, V, keep, dst, cap, S);
-        }
-        if (count < R || count > kStageKeys) {
-            if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
-            count = count > kStageKeys ? kStageKeys : count;
-        }
-        const int RR = R < count ? R : count;
-        if (count <= kLsdMax) {
-            // bucket counts are intact on the bucketed path (the radix path reuses them)
-            if (bucketed) dense_rank_keys(dst, count, T, shift, smin, S);
-            const int E = (count + kSelectThreads - 1) / kSelectThreads;
-            unsigned long long* B = S.stg;
-            switch (E) {
-            case 0:
-            case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
-            case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
-            case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
-            case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
-            case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
-            case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
-            case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
-            default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
+        const bool direct = staged && V <= kDirectMaxKeys && count >= R &&
+                            select_direct(S.stg, V, R, T, shift, smin, sel, S);
+        if (!direct) {
+            if (bucketed) {
+                const uint32_t lim = ((uint32_t)T + 1u) << shift;  // bucket <= T
+                auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
+                count = staged ? compact_stable(get_s, V, keep, dst, kLsdMax, S)
+                               : compact_stable(get_g, V, keep, dst, kLsdMax, S);
+            } else {
+                if (tid == 0) st.select_fallbacks += 1;
+                unsigned long long pmask, prefix;
+                if (staged) radix_threshold(get_s, V, R, S, pmask, prefix);
+                else radix_threshold(get_g, V, R, S, pmask, prefix);
+                auto keep = [=](unsigned long long k) { return (k & pmask) <= prefix; };
+                if (R > kLsdMax) dst = S.stg;  // only reached unstaged (K > kLsdMax)
+                const int cap = (R > kLsdMax) ? kStageKeys : kLsdMax;
+                count = staged ? compact_stable(get_s, V, keep, dst, cap, S)
+                               : compact_stable(get_g, V, keep, dst, cap, S);
             }
-        } else {
-            sort_and_emit(S.stg, count, RR, sel);
+            if (count < R || count > kStageKeys) {
+                if (tid == 0) atomicOr(&st.status, kStatusBadSelect);
+                count = count > kStageKeys ? kStageKeys : count;
+            }
+            const int RR = R < count ? R : count;
+            if (count <= kLsdMax) {
+                // bucket counts are intact on the bucketed path (the radix path reuses them)
+                if (bucketed) dense_rank_keys(dst, count, T, shift, smin, S);
+                const int E = (count + kSelectThreads - 1) / kSelectThreads;
+                unsigned long long* B = S.stg;
+                switch (E) {
+                case 0:
+                case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
+                case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
+                case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
+                case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
+                case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
+                case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
+                case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
+                default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
+                }
+            } else {
+                sort_and_emit(S.stg, count, RR, sel);
+            }
         }
     }
     __syncthreads();
