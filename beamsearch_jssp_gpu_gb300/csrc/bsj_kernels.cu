@@ -218,7 +218,7 @@ __device__ void apply_child(uint8_t* b, const Lay& L, const uint32_t* ops, int o
 // predecessor finish and the parent makespan.  Keys go to this CTA's chunk region at
 // positions reserved with a shared-memory counter.
 // ------------------------------------------------------------------------------------
-template <int NQ>
+template <int NQ, bool SMEM_NOISE>
 __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc& d, SegState& st,
                            const StepArgs& a, int c, int t, int lane, unsigned long long* kstage,
                            int* nv_out, const float* s_noise)
@@ -254,7 +254,8 @@ __device__ void expand_gpu(uint8_t* sb, uint8_t* cb, const Lay& L, const SegDesc
                 // (float)cmax / (float)ns + (float)(h % 1000) / 1e9f, IEEE round-to-nearest;
                 // the second quotient comes from a table of its 1000 possible values
                 const float base = __fdiv_rn(__int2float_rn(cm), fns);
-                const float sc = __fadd_rn(base, s_noise[noise_hash(seed_t, (uint32_t)c, (uint32_t)b) % 1000u]);
+                const uint32_t ni = noise_hash(seed_t, (uint32_t)c, (uint32_t)b) % 1000u;
+                const float sc = __fadd_rn(base, SMEM_NOISE ? s_noise[ni] : __ldg(s_noise + ni));
                 const uint32_t slot = (uint32_t)(c * L.n + b);
                 key[q] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
                 const uint32_t bit = 1u << (b & 31);
@@ -377,7 +378,9 @@ k_step(StepArgs a, int s)
 {
     constexpr int kRanksPerWarp = CH / kWarpsPerStepCta;
     extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ float s_noise[1000];
+    // noise quotients: small chunks read the plan's table through L1, 32-survivor chunks
+    // (more candidates per CTA) copy it into shared memory once
+    __shared__ float s_noise_tab[CH >= 32 ? 1000 : 1];
     __shared__ int s_nv[CH], s_pre[CH], s_kcnt, s_P;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint8_t* wbuf = smem + (size_t)warp * (kRanksPerWarp + 1) * a.sb_max;
@@ -387,8 +390,10 @@ k_step(StepArgs a, int s)
     unsigned long long* kstage = reinterpret_cast<unsigned long long*>(
         smem + (size_t)kWarpsPerStepCta * (kRanksPerWarp + 1) * a.sb_max);
     pdl_trigger();
-    for (int k = threadIdx.x; k < 1000; k += blockDim.x) s_noise[k] = __ldg(a.noise + k);
+    if constexpr (CH >= 32)
+        for (int k = threadIdx.x; k < 1000; k += blockDim.x) s_noise_tab[k] = __ldg(a.noise + k);
     pdl_wait();
+    const float* s_noise = CH >= 32 ? s_noise_tab : a.noise;
     for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
         const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
         const SegDesc& d = a.segs[seg];
@@ -476,7 +481,8 @@ k_step(StepArgs a, int s)
             if (compat) expand_compat<NQ>(sb, L, d, a, r, lane);
             else {
                 const int rl = r - q * CH;
-                expand_gpu<NQ>(sb, cb, L, d, st, a, r, s + 1, lane, kstage + (size_t)rl * nst, &s_nv[rl], s_noise);
+                expand_gpu<NQ, (CH >= 32)>(sb, cb, L, d, st, a, r, s + 1, lane, kstage + (size_t)rl * nst, &s_nv[rl],
+                                           s_noise);
             }
         }
         __syncthreads();
@@ -984,24 +990,80 @@ __device__ int dense_build(ForEach each, int T, int shift, uint32_t smin, const 
     return Dn;
 }
 
-__device__ bool dense_rank_keys(unsigned long long* A, int count, int T, int shift, uint32_t smin,
+// 4'. One stable counting pass over the compacted survivors by their dense score rank (at
+// most 256 distinct), scattered straight into `sel`.  The rank of each element comes from
+// the dense tables as it is loaded: the keys are not rewritten, no min/max pass, no second
+// buffer and no emit pass.  Elements p = warp*32*E + e*32 + lane (warps own contiguous
+// runs) are ranked in element order against per-warp 16-bit digit counters with
+// bit-ballot peer masks; a digit-major prefix over (digit, warp) gives the positions.
+template <int E>
+__device__ void dense_sort_emit(const unsigned long long* A, int count, int R, const DenseTables& D, uint32_t* sel,
                                 const SelSmem& S)
 {
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    DenseTables D;
-    D.occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
-    D.bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
-    D.wp = D.bm + kDenseWords;
-    auto each = [&](auto fn) {
-        for (int i = tid; i < count; i += nthr) fn(A[i]);
-    };
-    if (dense_build(each, T, shift, smin, S, D) < 0) return false;
-    for (int i = tid; i < count; i += nthr) {
-        const unsigned long long k = A[i];
-        A[i] = ((unsigned long long)D.rank_of((uint32_t)(k >> 32)) << 32) | (k & 0xFFFFFFFFull);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    uint16_t* wh = reinterpret_cast<uint16_t*>(S.hist);   // [32][256]
+    int* dtot = reinterpret_cast<int*>(S.tot);           // [256]
+    for (int i = tid; i < 32 * 256 / 2; i += blockDim.x) S.hist[i] = 0u;
+    __syncthreads();
+    uint32_t slot[E];
+    int dg[E], off[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int p = warp * 32 * E + e * 32 + lane;
+        const bool valid = p < count;
+        const unsigned long long x = valid ? A[p] : 0ull;
+        const int d = valid ? (int)D.rank_of((uint32_t)(x >> 32)) : 0;
+        unsigned grp = __ballot_sync(FULL_MASK, valid);
+#pragma unroll
+        for (int bit = 0; bit < 8; bit++) {
+            const unsigned bb = __ballot_sync(FULL_MASK, (d >> bit) & 1);
+            grp &= ((d >> bit) & 1) ? bb : ~bb;
+        }
+        const int r_in = __popc(grp & lt);
+        int b = 0;
+        if (valid) b = wh[warp * 256 + d];
+        __syncwarp();
+        if (valid && r_in == 0) wh[warp * 256 + d] = (uint16_t)(b + __popc(grp));
+        __syncwarp();
+        slot[e] = (uint32_t)(x & 0xFFFFFFFFull);
+        dg[e] = d;
+        off[e] = b + r_in;
     }
     __syncthreads();
-    return true;
+    if (tid < 256) {
+        int run = 0;
+        for (int w = 0; w < 32; w++) {
+            const int t = wh[w * 256 + tid];
+            wh[w * 256 + tid] = (uint16_t)run;
+            run += t;
+        }
+        dtot[tid] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int v8[8], sum = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { v8[u] = dtot[lane * 8 + u]; sum += v8[u]; }
+        int xx = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, xx, o);
+            if (lane >= o) xx += y;
+        }
+        int run = xx - sum;
+#pragma unroll
+        for (int u = 0; u < 8; u++) { dtot[lane * 8 + u] = run; run += v8[u]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int p = warp * 32 * E + e * 32 + lane;
+        if (p < count) {
+            const int pos = dtot[dg[e]] + (int)wh[warp * 256 + dg[e]] + off[e];
+            if (pos < R) sel[pos] = slot[e];
+        }
+    }
 }
 
 // 4. stable LSD radix sort of `count` (<= kLsdMax) keys by their score bits, first R out.
@@ -1589,20 +1651,52 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
             }
             const int RR = R < count ? R : count;
             if (count <= kLsdMax) {
-                // bucket counts are intact on the bucketed path (the radix path reuses them)
-                if (bucketed) dense_rank_keys(dst, count, T, shift, smin, S);
                 const int E = (count + kSelectThreads - 1) / kSelectThreads;
-                unsigned long long* B = S.stg;
-                switch (E) {
-                case 0:
-                case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
-                case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
-                case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
-                case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
-                case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
-                case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
-                case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
-                default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
+                int nd = -1;
+                DenseTables D;
+                if (bucketed) {
+                    // bucket counts are intact on the bucketed path (the radix path reuses them)
+                    D.occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
+                    D.bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
+                    D.wp = D.bm + kDenseWords;
+                    auto each = [&](auto fn) {
+                        for (int i = tid; i < count; i += kSelectThreads) fn(dst[i]);
+                    };
+                    nd = dense_build(each, T, shift, smin, S, D);
+                }
+                if (nd >= 0 && nd <= 256) {
+                    switch (E) {
+                    case 0:
+                    case 1: dense_sort_emit<1>(dst, count, RR, D, sel, S); break;
+                    case 2: dense_sort_emit<2>(dst, count, RR, D, sel, S); break;
+                    case 3: dense_sort_emit<3>(dst, count, RR, D, sel, S); break;
+                    case 4: dense_sort_emit<4>(dst, count, RR, D, sel, S); break;
+                    case 5: dense_sort_emit<5>(dst, count, RR, D, sel, S); break;
+                    case 6: dense_sort_emit<6>(dst, count, RR, D, sel, S); break;
+                    case 7: dense_sort_emit<7>(dst, count, RR, D, sel, S); break;
+                    default: dense_sort_emit<8>(dst, count, RR, D, sel, S); break;
+                    }
+                } else {
+                    if (nd > 256) {
+                        // more distinct scores than one 8-bit pass: ranks into the keys, LSD passes
+                        for (int i = tid; i < count; i += kSelectThreads) {
+                            const unsigned long long k = dst[i];
+                            dst[i] = ((unsigned long long)D.rank_of((uint32_t)(k >> 32)) << 32) | (k & 0xFFFFFFFFull);
+                        }
+                        __syncthreads();
+                    }
+                    unsigned long long* B = S.stg;
+                    switch (E) {
+                    case 0:
+                    case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
+                    case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
+                    case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
+                    case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
+                    case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
+                    case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
+                    case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
+                    default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
+                    }
                 }
             } else {
                 sort_and_emit(S.stg, count, RR, sel);
