@@ -10,11 +10,15 @@
 // unique result.  All device buffers are zeroed first, as a fresh process's first
 // allocation reads.
 //
-// Usage: ref_gpu_harness v1|v2 <cubin> <instance file> <K> <best_known> <seed>
-// Prints one JSON object: {"makespan": M, "sequence": [...]}.
+// Usage: ref_gpu_harness v1|v2 <cubin> <instance file> <K> <best_known> <seed> [time]
+// Prints one JSON object: {"makespan": M, "sequence": [...]}; with `time`, also the device
+// time of the reference's two kernels summed over the search (CUDA events around every
+// launch), "kernel_ms": [first, second], and the host time of the substituted sort,
+// "host_sort_ms" -- a lower bound of the reference's own GPU time, which adds CUB's sort.
 #include <cuda.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -73,10 +77,11 @@ static CUfunction find_kernel(CUmodule mod, const char* needle)
 
 int main(int argc, char** argv)
 {
-    if (argc != 7) {
-        std::fprintf(stderr, "usage: %s v1|v2 cubin instance K best_known seed\n", argv[0]);
+    if (argc != 7 && !(argc == 8 && std::string(argv[7]) == "time")) {
+        std::fprintf(stderr, "usage: %s v1|v2 cubin instance K best_known seed [time]\n", argv[0]);
         return 1;
     }
+    const bool timing = argc == 8;
     const bool v2 = std::string(argv[1]) == "v2";
     const int K = std::atoi(argv[4]);
     const int best_known = std::atoi(argv[5]);
@@ -141,6 +146,14 @@ int main(int argc, char** argv)
     root[L.off_ready_count] = n;
     CK(cuMemcpyHtoD(beam_a, root.data(), S * 4));
 
+    CUevent ev[4];
+    for (CUevent& e : ev) CK(cuEventCreate(&e, CU_EVENT_DEFAULT));
+    double kms[2] = {0.0, 0.0}, sort_ms = 0.0;
+    auto elapsed = [&](CUevent a, CUevent b) {
+        float t = 0.f;
+        CK(cuEventElapsedTime(&t, a, b));
+        return (double)t;
+    };
     CUdeviceptr cur = beam_a, nxt = beam_b;
     int P = 1;
     const unsigned smem = (unsigned)((S + n + 1) * 4);
@@ -151,6 +164,7 @@ int main(int argc, char** argv)
         int step_seed = (int)((unsigned)seed + (unsigned)step);
         int num_machines = m, num_ops_tot = nbop, total_real = N, bpc = n;
         Layout lay = L;
+        if (timing) CK(cuEventRecord(ev[0], 0));
         if (!v2) {
             void* args[] = {&cur, &child, &scores, &indices, &gbest, &best_sol, &P, &bpc, &lay,
                             &num_machines, &num_ops_tot, &total_real, &step_seed};
@@ -160,7 +174,10 @@ int main(int argc, char** argv)
                             &num_machines, &num_ops_tot, &total_real, &step_seed};
             CK(cuLaunchKernel(k_first, P, 1, 1, n, 1, 1, smem, 0, args, nullptr));
         }
+        if (timing) CK(cuEventRecord(ev[1], 0));
         CK(cuCtxSynchronize());
+        if (timing) kms[0] += elapsed(ev[0], ev[1]);
+        const auto t_sort = std::chrono::steady_clock::now();
         CK(cuMemcpyDtoH(h_scores.data(), scores, (size_t)total * 4));
         CK(cuMemcpyDtoH(h_idx.data(), indices, (size_t)total * 4));
         std::iota(order.begin(), order.begin() + total, 0);
@@ -168,7 +185,9 @@ int main(int argc, char** argv)
                          [&](int x, int y) { return h_scores[x] < h_scores[y]; });
         for (int r = 0; r < total; r++) h_sorted[r] = h_idx[order[r]];
         CK(cuMemcpyHtoD(sorted, h_sorted.data(), (size_t)total * 4));
+        sort_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_sort).count();
         int gather = std::min(total, K);
+        if (timing) CK(cuEventRecord(ev[2], 0));
         int threads = 256, blocks = (gather + threads - 1) / threads;
         if (!v2) {
             int sints = (int)S;
@@ -180,7 +199,9 @@ int main(int argc, char** argv)
             CK(cuLaunchKernel(k_second, blocks, 1, 1, threads, 1, 1, 0, 0, args, nullptr));
             std::swap(cur, nxt);
         }
+        if (timing) CK(cuEventRecord(ev[3], 0));
         CK(cuCtxSynchronize());
+        if (timing) kms[1] += elapsed(ev[2], ev[3]);
         P = gather;
     }
     int best = 500000;
@@ -189,7 +210,9 @@ int main(int argc, char** argv)
     CK(cuMemcpyDtoH(sol.data(), best_sol, S * 4));
     std::printf("{\"makespan\": %d, \"sequence\": [", best);
     for (int t = 0; t < N; t++) std::printf("%s%d", t ? ", " : "", best < 500000 ? sol[L.off_sequence + t] : 0);
-    std::printf("]}\n");
+    if (timing) std::printf("], \"kernel_ms\": [%.3f, %.3f], \"host_sort_ms\": %.3f}\n", kms[0], kms[1], sort_ms);
+    else std::printf("]}\n");
+    for (CUevent& e : ev) CK(cuEventDestroy(e));
     CK(cuModuleUnload(mod));
     CK(cuDevicePrimaryCtxRelease(dev));
     return 0;
