@@ -992,23 +992,23 @@ __device__ int dense_build(ForEach each, int T, int shift, uint32_t smin, const 
 
 // 4'. One stable counting pass over the compacted survivors by their dense score rank (at
 // most 256 distinct), scattered straight into `sel`.  The rank of each element comes from
-// the dense tables as it is loaded: the keys are not rewritten, no min/max pass, no second
-// buffer and no emit pass.  Elements p = warp*32*E + e*32 + lane (warps own contiguous
-// runs) are ranked in element order against per-warp 16-bit digit counters with
-// bit-ballot peer masks; a digit-major prefix over (digit, warp) gives the positions.
-template <int E>
-__device__ void dense_sort_emit(const unsigned long long* A, int count, int R, const DenseTables& D, uint32_t* sel,
-                                const SelSmem& S)
+// the dense tables as it is loaded: no min/max pass, no second buffer, no emit pass.
+// Elements p = warp*32*E + e*32 + lane (warps own contiguous runs, E = ceil(count/1024))
+// are ranked in element order against per-warp 16-bit digit counters with bit-ballot peer
+// masks; each element's (rank, offset) goes back into its own A slot (bits 63..48 rank,
+// 47..32 offset) so the loops stay rolled; a digit-major prefix over (digit, warp) gives
+// the positions.
+__device__ void dense_sort_emit(unsigned long long* A, int count, int R, const DenseTables& D, uint32_t* sel,
+                                       const SelSmem& S)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1u;
+    const int E = (count + kSelectThreads - 1) / kSelectThreads;
     uint16_t* wh = reinterpret_cast<uint16_t*>(S.hist);   // [32][256]
     int* dtot = reinterpret_cast<int*>(S.tot);           // [256]
     for (int i = tid; i < 32 * 256 / 2; i += blockDim.x) S.hist[i] = 0u;
     __syncthreads();
-    uint32_t slot[E];
-    int dg[E], off[E];
-#pragma unroll
+#pragma unroll 1
     for (int e = 0; e < E; e++) {
         const int p = warp * 32 * E + e * 32 + lane;
         const bool valid = p < count;
@@ -1026,9 +1026,8 @@ __device__ void dense_sort_emit(const unsigned long long* A, int count, int R, c
         __syncwarp();
         if (valid && r_in == 0) wh[warp * 256 + d] = (uint16_t)(b + __popc(grp));
         __syncwarp();
-        slot[e] = (uint32_t)(x & 0xFFFFFFFFull);
-        dg[e] = d;
-        off[e] = b + r_in;
+        if (valid)
+            A[p] = ((unsigned long long)d << 48) | ((unsigned long long)(b + r_in) << 32) | (x & 0xFFFFFFFFull);
     }
     __syncthreads();
     if (tid < 256) {
@@ -1056,12 +1055,14 @@ __device__ void dense_sort_emit(const unsigned long long* A, int count, int R, c
         for (int u = 0; u < 8; u++) { dtot[lane * 8 + u] = run; run += v8[u]; }
     }
     __syncthreads();
-#pragma unroll
+#pragma unroll 1
     for (int e = 0; e < E; e++) {
         const int p = warp * 32 * E + e * 32 + lane;
         if (p < count) {
-            const int pos = dtot[dg[e]] + (int)wh[warp * 256 + dg[e]] + off[e];
-            if (pos < R) sel[pos] = slot[e];
+            const unsigned long long x = A[p];
+            const int dg = (int)(x >> 48);
+            const int pos = dtot[dg] + (int)wh[warp * 256 + dg] + (int)((x >> 32) & 0xFFFFull);
+            if (pos < R) sel[pos] = (uint32_t)(x & 0xFFFFFFFFull);
         }
     }
 }
@@ -1665,17 +1666,7 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
                     nd = dense_build(each, T, shift, smin, S, D);
                 }
                 if (nd >= 0 && nd <= 256) {
-                    switch (E) {
-                    case 0:
-                    case 1: dense_sort_emit<1>(dst, count, RR, D, sel, S); break;
-                    case 2: dense_sort_emit<2>(dst, count, RR, D, sel, S); break;
-                    case 3: dense_sort_emit<3>(dst, count, RR, D, sel, S); break;
-                    case 4: dense_sort_emit<4>(dst, count, RR, D, sel, S); break;
-                    case 5: dense_sort_emit<5>(dst, count, RR, D, sel, S); break;
-                    case 6: dense_sort_emit<6>(dst, count, RR, D, sel, S); break;
-                    case 7: dense_sort_emit<7>(dst, count, RR, D, sel, S); break;
-                    default: dense_sort_emit<8>(dst, count, RR, D, sel, S); break;
-                    }
+                    dense_sort_emit(dst, count, RR, D, sel, S);
                 } else {
                     if (nd > 256) {
                         // more distinct scores than one 8-bit pass: ranks into the keys, LSD passes
