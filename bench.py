@@ -399,7 +399,7 @@ def batched_stream(ctx, count: int = 256, seed: int = 1) -> dict:
             "expanded_per_s": sum(r["expanded"] for r in out) / t_batch}
 
 
-def served_stream(ctx, device: int, count: int = 400, rates=(150.0, 1000.0), inflight: int = 48,
+def served_stream(ctx, device: int, count: int = 400, rates=(150.0, 1000.0), inflight: int = 96,
                   seed: int = 5) -> dict:
     """Open-loop Poisson arrivals served by bsj_server (continuous batching), at a rate the
     server sustains and at one it cannot (queueing), against the plain path solving the same
