@@ -24,9 +24,11 @@ namespace bsj {
 // ------------------------------------------------------------------------------------
 // helpers
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ int find_seg(const int32_t* prefix, int nseg, int flat)
+// The beam holding flat index `flat` among the launch's beams [lo, hi) (prefix = per-beam
+// prefix sums).  A launch is usually one beam group of few beams -- often one -- so the
+// search is over that range, not over every beam of the plan.
+__device__ __forceinline__ int find_seg(const int32_t* prefix, int lo, int hi, int flat)
 {
-    int lo = 0, hi = nseg;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
         if (__ldg(prefix + mid) <= flat) lo = mid; else hi = mid;
@@ -395,7 +397,7 @@ k_step(StepArgs a, int s)
     pdl_wait();
     const float* s_noise = CH >= 32 ? s_noise_tab : a.noise;
     for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
-        const int seg = find_seg(a.chunk_prefix, a.nseg, chunk);
+        const int seg = find_seg(a.chunk_prefix, a.seg_lo, a.seg_hi, chunk);
         const SegDesc& d = a.segs[seg];
         if (d.nq != NQ || s >= d.N - 1) continue;
         SegState& st = a.st[seg];
@@ -521,7 +523,7 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a,
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = gridDim.x * kWarpsPerStepCta;
     for (int flat = a.rank_lo + blockIdx.x * kWarpsPerStepCta + warp; flat < a.rank_hi; flat += nw) {
-        const int seg = find_seg(a.rank_prefix, a.nseg, flat);
+        const int seg = find_seg(a.rank_prefix, a.seg_lo, a.seg_hi, flat);
         const SegDesc& d = a.segs[seg];
         if (d.mode != MODE_V1 || s >= d.N - 1) continue;
         const int r = flat - __ldg(a.rank_prefix + seg);
