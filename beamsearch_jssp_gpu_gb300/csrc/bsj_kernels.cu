@@ -370,12 +370,16 @@ template <int NQ, int CH>
 #ifndef BSJ_STEP_MIN_BLOCKS
 #define BSJ_STEP_MIN_BLOCKS 4
 #endif
-#ifndef BSJ_STEP_MIN_BLOCKS_NQ2
-#define BSJ_STEP_MIN_BLOCKS_NQ2 BSJ_STEP_MIN_BLOCKS
+#ifndef BSJ_STEP_MIN_BLOCKS_WIDE
+#define BSJ_STEP_MIN_BLOCKS_WIDE 6
 #endif
-// four resident CTAs per SM (64 registers); the n > 64 instance needs more registers
+// Resident CTAs per SM (register budget): four (64 registers) by default, three for
+// n > 64.  For 33 <= n <= 64 the 16- and 32-survivor chunks -- which the chunk rule picks
+// for wide levels, where the GPU's k_step throughput bounds a level -- take six (42
+// registers): 37.0 vs 38.1 ms on 8 beams x K=4096 at 50x20; the 8-survivor chunk, picked
+// for narrow latency-bound levels, keeps four (six cost a single such beam 4-5 %).
 __global__ void __launch_bounds__(kWarpsPerStepCta * 32,
-                                  NQ == 4 ? 3 : NQ == 2 ? BSJ_STEP_MIN_BLOCKS_NQ2 : BSJ_STEP_MIN_BLOCKS)
+                                  NQ == 4 ? 3 : (NQ == 2 && CH >= 16) ? BSJ_STEP_MIN_BLOCKS_WIDE : BSJ_STEP_MIN_BLOCKS)
 k_step(StepArgs a, int s)
 {
     constexpr int kRanksPerWarp = CH / kWarpsPerStepCta;
