@@ -537,6 +537,41 @@ def chunk_sweep(args) -> int:
     return 0
 
 
+def solve_times(args) -> int:
+    """Single searches on the GPU path, one beam per plan (default chunk rule), in the gpu
+    modes: 20x15 K=1024 and 50x20 K=4096, synthetic instance seed 0, search seed 0 -- the
+    cases the reference's own gpu kernels are timed on by the oracle's timing script.
+    CUDA events on an explicit stream, median of `--steps` runs after `--warmup`."""
+    import torch
+
+    from beamsearch_jssp_gpu_gb300 import BeamSpec, Context, synthetic_instance
+
+    ctx = Context(0)
+    stream = torch.cuda.Stream()
+    for n, m, K in ((20, 15, 1024), (50, 20, 4096)):
+        mc, du = synthetic_instance(n, m, 0)
+        for mode in ("v2", "v1"):
+            plan = ctx.plan([(mc, du)], [BeamSpec(mode, K, 500000, 0, 0, -1)])
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    plan.run(stream.cuda_stream)
+                times = []
+                for _ in range(args.steps):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    plan.run(stream.cuda_stream)
+                    e1.record(stream)
+                    e1.synchronize()
+                    times.append(e0.elapsed_time(e1))
+            r = plan.results(with_sequence=False)[0]
+            print(json.dumps({"solver": f"engine {mode}", "jobs": n, "machines": m, "beam_width": K, "seed": 0,
+                              "ms_per_search": statistics.median(times), "makespan": r["makespan"]}), flush=True)
+            plan.close()
+    ctx.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -548,7 +583,11 @@ def main() -> int:
     ap.add_argument("--k-sweep", action="store_true", help="time vs beam width (20x15, gpu-v1), one line per K")
     ap.add_argument("--chunk-sweep", action="store_true",
                     help="ms per search of each k_step chunk size over a set of shapes (autotuner data)")
+    ap.add_argument("--solve-times", action="store_true",
+                    help="single gpu-v1/v2 searches (20x15 K=1024, 50x20 K=4096): ms per search")
     args = ap.parse_args()
+    if args.solve_times:
+        return solve_times(args)
     if args.k_sweep:
         return k_sweep(args)
     if args.chunk_sweep:
