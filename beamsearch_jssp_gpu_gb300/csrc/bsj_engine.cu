@@ -212,17 +212,18 @@ int chunk_var_of(int chunk)
 
 // Default rule for one beam group: `ranks` = survivors per level of the whole plan (all
 // groups run at once), `nq` = ceil(n/32) class holding most of the group's survivors,
-// `kmax` = the group's widest beam.  Measured on GB300 (bench.py --chunk-sweep, gpu-v2,
+// `granks` = the group's own survivors per level.  Measured on GB300 (bench.py --chunk-sweep, gpu-v2,
 // 18 shapes from 10x5 K=256 to 100x20 8x4096; the rule picks the fastest on all): up to
 // 8 192 survivors per level the level is narrow and 8 per CTA spreads it over the most SMs
 // (3-30 % faster than 16), except for n > 64 at 4 096 and more, where per-CTA set-up
 // dominates and 32 wins; wider plans -- several beams at once -- run 16 per CTA (the
-// n <= 64 kernels with 16 and 32 keep six CTAs per SM resident), and 32 where one beam
-// alone is wider than 8 192 or n > 64.
-int rule_chunk_var(int64_t ranks, int nq, int kmax)
+// n <= 64 kernels with 16 and 32 keep six CTAs per SM resident), and 32 where the group
+// alone holds more than 8 192 (one wide beam, or several beams in lockstep: 8 beams of
+// 4 096 at 50x20 as 2 groups, 44.3 vs 49.5 ms) or n > 64.
+int rule_chunk_var(int64_t ranks, int nq, int64_t granks)
 {
     if (ranks <= 8192) return chunk_var_of((nq == 4 && ranks >= 4096) ? 32 : 8);
-    return chunk_var_of((nq == 4 || kmax > 8192) ? 32 : 16);
+    return chunk_var_of((nq == 4 || granks > 8192) ? 32 : 16);
 }
 
 // With `bytes_only` non-null, computes the plan's device footprint into it and allocates
@@ -531,13 +532,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     // this device, else the rule
     for (auto& gr : p->groups) {
         int64_t per_nq[5] = {0, 0, 0, 0, 0};
-        int kmax = 0;
-        for (int b = gr.args.seg_lo; b < gr.args.seg_hi; b++) {
-            per_nq[p->segs[b].nq] += p->segs[b].K;
-            kmax = std::max(kmax, p->segs[b].K);
-        }
+        for (int b = gr.args.seg_lo; b < gr.args.seg_hi; b++) per_nq[p->segs[b].nq] += p->segs[b].K;
         const int nq = per_nq[4] > per_nq[2] && per_nq[4] > per_nq[1] ? 4 : (per_nq[2] > per_nq[1] ? 2 : 1);
-        gr.rule_var = rule_chunk_var(p->total_ranks, nq, kmax);
+        gr.rule_var = rule_chunk_var(p->total_ranks, nq, per_nq[1] + per_nq[2] + per_nq[4]);
     }
     {
         const int v = tuned_chunk(ctx, p->shape);
