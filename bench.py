@@ -75,15 +75,18 @@ def _cpu_worker(args):
     return r["expanded"], time.perf_counter() - t0
 
 
-def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS) -> dict:
+def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS, pool=None) -> dict:
+    """One bounded sample on the host cores, a process per beam (`pool`: reuse an open
+    spawn pool of `procs` workers)."""
     from oracle import oracle as O
 
-    O.build(ref=False)
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        t0 = time.perf_counter()
-        out = pool.map(_cpu_worker, [(s, levels) for s in seeds])
-        wall = time.perf_counter() - t0
+    if pool is None:
+        O.build(ref=False)
+        with mp.get_context("spawn").Pool(procs) as own:
+            return cpu_sample(procs, seeds, levels, own)
+    t0 = time.perf_counter()
+    out = pool.map(_cpu_worker, [(s, levels) for s in seeds])
+    wall = time.perf_counter() - t0
     expanded = sum(e for e, _ in out)
     busy = max(t for _, t in out)
     return dict(expanded=expanded, wall=wall, busy=busy, value=expanded / busy)
@@ -96,15 +99,23 @@ def reference_arm(args) -> int:
         return 0
     procs = max(1, min(BEAMS, os.cpu_count() or 1))
     seeds = list(range(BEAMS))
-    for _ in range(args.warmup):
-        cpu_sample(procs, seeds, levels=20)
+    # each step a bounded sample: ~10 000 levels of the 8 beams over the whole run (a full
+    # 1 000-level search per step at 10 steps), 100 to 1 000 levels per step, so any
+    # --steps finishes in about a minute and a half on the GPU host's cores
+    levels = max(100, min(CPU_SAMPLE_LEVELS, 10000 // max(1, args.steps)))
+    from oracle import oracle as O
+
+    O.build(ref=False)
     vals, times = [], []
-    for _ in range(args.steps):
-        r = cpu_sample(procs, seeds)
-        vals.append(r["value"])
-        times.append(r["busy"])
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for _ in range(args.warmup):
+            cpu_sample(procs, seeds, levels=20, pool=pool)
+        for _ in range(args.steps):
+            r = cpu_sample(procs, seeds, levels=levels, pool=pool)
+            vals.append(r["value"])
+            times.append(r["busy"])
     value = sum(vals) / len(vals)
-    sample = (f"levels 0-{CPU_SAMPLE_LEVELS - 1} of each of {BEAMS} beams (seeds 0-{BEAMS - 1}), "
+    sample = (f"levels 0-{levels - 1} of each of {BEAMS} beams (seeds 0-{BEAMS - 1}), "
               f"{procs} processes, per step")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times),
