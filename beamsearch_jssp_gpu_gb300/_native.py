@@ -34,9 +34,16 @@ EXPORTED = [
     "bsj_plan_estimate", "bsj_plan_device_bytes", "bsj_plan_update",
     "bsj_server_create", "bsj_server_destroy", "bsj_submit", "bsj_poll", "bsj_wait", "bsj_server_get_stats",
     "bsj_plan_autotune", "bsj_plan_set_chunk", "bsj_plan_chunk", "bsj_set_autotune",
+    "bsj_plan_set_select_route", "bsj_plan_select_routes", "bsj_server_prepare",
 ]
-CHUNK_SIZES = (8, 16, 32)  # k_step work-unit sizes (survivors per thread block)
-CHUNK_CANDIDATES = (0, 8, 16, 32)  # what the autotuner chooses among: 0 = the default rule
+# top-K selection routes (include/bsj.h BSJ_SELECT_* / BSJ_ROUTE_*)
+SELECT = {"force_large": 1, "no_large": 2, "no_direct": 4, "radix": 8, "no_dense": 16, "rank_lsd": 32,
+          "bitonic": 64}
+ROUTE = {"large": 1, "direct": 2, "bucket": 4, "radix": 8, "dense": 16, "rank_lsd": 32, "raw_lsd": 64,
+         "bitonic": 128}
+CHUNK_SIZES = (8, 16, 32)  # k_step work-unit sizes (survivors per thread block), warp per survivor
+THREAD_FORMS = (1, 2)      # k_step thread per survivor: 16-byte-load / bulk-copy staging
+CHUNK_CANDIDATES = (0, 8, 16, 32, 1, 2)  # what the autotuner chooses among: 0 = the default rule
 
 
 class ServerConfig(ctypes.Structure):
@@ -45,14 +52,16 @@ class ServerConfig(ctypes.Structure):
 
 
 class RequestTimes(ctypes.Structure):
-    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double)]
+    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("built_plan", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in ("submitted", "completed", "plans_built", "plans_reused",
                                                "peak_inflight", "peak_device_bytes", "budget_bytes",
                                                "pending")] + \
-               [(k, ctypes.c_double) for k in ("build_ms", "update_ms", "launch_ms", "collect_ms")]
+               [(k, ctypes.c_double) for k in ("build_ms", "update_ms", "launch_ms", "collect_ms")] + \
+               [("plans_prepared", ctypes.c_int64)]
 
 
 class BsjError(RuntimeError):
@@ -126,6 +135,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     # autotuning of the k_step chunk size
     L.bsj_plan_autotune.argtypes = [vp, vp, ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_float)]
     L.bsj_plan_set_chunk.argtypes = [vp, ctypes.c_int32]
+    L.bsj_plan_set_select_route.argtypes = [vp, ctypes.c_int32]
+    L.bsj_plan_select_routes.argtypes = [vp, P(ctypes.c_uint32)]
     L.bsj_plan_chunk.argtypes = [vp]
     L.bsj_plan_chunk.restype = ctypes.c_int32
     L.bsj_set_autotune.argtypes = [vp, ctypes.c_int32]
@@ -152,15 +163,16 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     L.bsj_poll.argtypes = [vp, ctypes.c_uint64, P(Result), P(RequestTimes), P(ctypes.c_int32)]
     L.bsj_wait.argtypes = [vp, ctypes.c_uint64, P(Result), P(RequestTimes)]
     L.bsj_server_get_stats.argtypes = [vp, P(ServerStats)]
+    L.bsj_server_prepare.argtypes = [vp, P(Instance), P(Beam), ctypes.c_int32]
     for name in ("bsj_plan_estimate", "bsj_plan_update", "bsj_server_create", "bsj_submit", "bsj_poll",
-                 "bsj_wait", "bsj_server_get_stats"):
+                 "bsj_wait", "bsj_server_get_stats", "bsj_server_prepare"):
         getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_instance_resolve", "bsj_instance_read", "bsj_schedule_decode", "bsj_device_count"):
         getattr(L, name).restype = ctypes.c_int
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
                  "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
                  "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_plan_autotune", "bsj_plan_set_chunk",
-                 "bsj_set_autotune"):
+                 "bsj_set_autotune", "bsj_plan_set_select_route", "bsj_plan_select_routes"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

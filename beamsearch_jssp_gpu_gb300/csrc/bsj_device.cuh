@@ -54,6 +54,21 @@ constexpr int kHeapMaxChunk = 32;     // parents per k_heap chunk (at most)
 constexpr int kStatusBadLineage = 1;
 constexpr int kStatusBadSelect = 2;
 
+// Routes of k_select's top-K selection.  StepArgs::select_force (0 = the normal choice by
+// level size) forces a level onto a route, so tests can run every route on small
+// levels; the result never depends on the route.
+constexpr int kSelForceLarge = 1;   // global-memory large-level path whatever the level size
+constexpr int kSelNoLarge = 2;      // never the large-level path
+constexpr int kSelNoDirect = 4;     // no direct staged path: compact the survivors first
+constexpr int kSelForceRadix = 8;   // MSD radix select of the R-th key, not the bucket threshold
+constexpr int kSelNoDense = 16;     // LSD passes on the raw score bits (no dense ranks)
+constexpr int kSelRankLsd = 32;     // dense ranks written into the keys, then LSD passes
+constexpr int kSelBitonic = 64;     // block bitonic sort of the survivors
+constexpr int kSelAll = 127;
+// Routes the levels of a beam took (SegState::select_paths, OR over the levels).
+constexpr uint32_t kPathLarge = 1, kPathDirect = 2, kPathBucket = 4, kPathRadix = 8, kPathDense = 16,
+                   kPathRankLsd = 32, kPathRawLsd = 64, kPathBitonic = 128;
+
 struct SegDesc {
     int32_t n, m, N, K;
     int32_t mode;
@@ -94,6 +109,7 @@ struct SegState {
     int32_t levels;
     int32_t makespan;
     int32_t found;
+    uint32_t select_paths;  // kPath* bits of the selection routes taken
     uint32_t rng_i;       // ICH/PMS rand() stream: position of the next value, in [34, 68)
     uint32_t rng[34];
 };

@@ -50,11 +50,12 @@ struct bsj_plan {
     int maxN = 0;
     int total_ranks = 0;
     int nq_mask = 0;
-    // k_step work unit (survivors per CTA): variant 0 runs every group with the chunk size
-    // the default rule gives it (Group::rule_var), variant 1 + v every group with
-    // kChunkSizes[v].  Set by the default, a tuning-table hit, bsj_plan_autotune or
-    // bsj_plan_set_chunk.
+    // k_step form: variant 0 runs every group with the step variant the default rule gives
+    // it (Group::rule_var), variant 1 + v every group with step variant v (kStepVariant*:
+    // warp per survivor with 8/16/32 per CTA, or thread per survivor).  Set by the
+    // default, a tuning-table hit, bsj_plan_autotune or bsj_plan_set_chunk.
     int variant = 0;
+    int select_force = 0;   // kSel* route flags of k_select (bsj_plan_set_select_route)
     int total_chunks[kNumChunkSizes] = {};
     int gather_grid = 1;
     int sort_cap = 0;
@@ -65,9 +66,10 @@ struct bsj_plan {
     struct Group {
         StepArgs args;   // chunk fields are filled per chunk size by group_args()
         int maxN = 0, nq_mask = 0, gather_grid = 1;
-        int rule_var = 1;  // chunk size (index into kChunkSizes) of the default rule
-        int step_grid[kNumChunkSizes] = {};
+        int rule_var = 1;  // step variant (index into kStepVariant*) of the default rule
+        int step_grid[kNumStepVariants] = {};
         bool has_v1 = false, has_gpu = false, has_compat = false;
+        bool thread_ok = false;  // every beam gpu-v2 / clean: thread-per-survivor k_step applies
     };
     std::vector<Group> groups;
     cudaEvent_t fork = nullptr;
@@ -95,7 +97,7 @@ struct bsj_plan {
     size_t beam_bytes = 0, slot_bytes = 0;
     StepArgs args{};
     // graphs per chunk variant: [0] plain, [1] with timing events recorded around each launch
-    cudaGraphExec_t graph[kNumChunkSizes + 1][2] = {};
+    cudaGraphExec_t graph[kNumStepVariants + 1][2] = {};
     // timing
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -510,16 +512,23 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             gr.args.seg_hi = hi;
             gr.args.rank_lo = p->prefix[lo];
             gr.args.rank_hi = p->prefix[hi];
+            gr.thread_ok = true;
             for (int b = lo; b < hi; b++) {
                 const SegDesc& d = p->segs[b];
                 gr.maxN = std::max(gr.maxN, d.N);
                 gr.nq_mask |= 1 << d.nq;
                 if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
                 if (d.mode <= BSJ_MODE_CLEAN) gr.has_gpu = true; else gr.has_compat = true;
+                if (d.mode != BSJ_MODE_V2 && d.mode != BSJ_MODE_CLEAN) gr.thread_ok = false;
             }
-            // k_step: one CTA per chunk
-            for (int v = 0; v < kNumChunkSizes; v++)
-                gr.step_grid[v] = std::max(1, std::min(p->cprefix[v][hi] - p->cprefix[v][lo], 65535));
+            // k_step: one CTA per chunk (warp per survivor), one warp per 32-survivor chunk
+            // (thread per survivor)
+            for (int v = 0; v < kNumStepVariants; v++) {
+                const int ci = chunk_var_of(kStepVariantChunk[v]);
+                int g = p->cprefix[ci][hi] - p->cprefix[ci][lo];
+                if (kStepVariantThread[v] && gr.thread_ok) g = (g + kTStepWarpsPerCta - 1) / kTStepWarpsPerCta;
+                gr.step_grid[v] = std::max(1, std::min(g, 65535));
+            }
             const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
             gr.gather_grid = std::max(1, std::min(wr, ctx->sm_count * 8));
             p->groups.push_back(gr);
@@ -544,22 +553,25 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     return BSJ_OK;
 }
 
-// Chunk size (index into kChunkSizes) group `gr` runs with under the plan's variant.
+// Step variant (index into kStepVariant*) group `gr` runs with under the plan's variant.
 int group_var(const bsj_plan* p, const bsj_plan::Group& gr)
 {
     return p->variant == 0 ? gr.rule_var : p->variant - 1;
 }
 
-// The launch arguments of group `gr` (whole plan: nullptr) for chunk size kChunkSizes[v].
+// The launch arguments of group `gr` (whole plan: nullptr) for step variant v.
 StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
 {
     StepArgs a = gr ? gr->args : p->args;
     const int lo = gr ? a.seg_lo : 0, hi = gr ? a.seg_hi : p->nseg;
-    a.chunk = kChunkSizes[v];
-    a.chunk_prefix = p->d_cprefix + (size_t)v * (p->nseg + 1);
-    a.chunk_lo = p->cprefix[v][lo];
-    a.chunk_hi = p->cprefix[v][hi];
-    a.total_chunks = p->total_chunks[v];
+    const int ci = chunk_var_of(kStepVariantChunk[v]);
+    a.chunk = kStepVariantChunk[v];
+    a.thread_step = (gr && gr->thread_ok) ? kStepVariantThread[v] : 0;
+    a.select_force = p->select_force;
+    a.chunk_prefix = p->d_cprefix + (size_t)ci * (p->nseg + 1);
+    a.chunk_lo = p->cprefix[ci][lo];
+    a.chunk_hi = p->cprefix[ci][hi];
+    a.total_chunks = p->total_chunks[ci];
     return a;
 }
 
@@ -1006,13 +1018,55 @@ bsj_status bsj_plan_set_chunk(bsj_plan* p, int32_t chunk)
 {
     if (!p) return BSJ_ERR_INVALID;
     if (chunk == 0) { p->variant = 0; return BSJ_OK; }
-    const int v = chunk_var_of(chunk);
-    if (v < 0) return fail(p->ctx, BSJ_ERR_INVALID, "chunk must be 0 (default rule), 8, 16 or 32");
-    p->variant = 1 + v;
+    for (int v = 0; v < kNumStepVariants; v++) {
+        if (kStepVariantCode[v] == chunk) {
+            p->variant = 1 + v;
+            return BSJ_OK;
+        }
+    }
+    return fail(p->ctx, BSJ_ERR_INVALID,
+                "chunk must be 0 (default rule), 8, 16, 32 (warp per survivor) or 1, 2 (thread per survivor)");
+}
+
+static_assert(BSJ_SELECT_FORCE_LARGE == kSelForceLarge && BSJ_SELECT_NO_LARGE == kSelNoLarge &&
+              BSJ_SELECT_NO_DIRECT == kSelNoDirect && BSJ_SELECT_RADIX == kSelForceRadix &&
+              BSJ_SELECT_NO_DENSE == kSelNoDense && BSJ_SELECT_RANK_LSD == kSelRankLsd &&
+              BSJ_SELECT_BITONIC == kSelBitonic, "route flags of bsj.h and the kernels differ");
+static_assert(BSJ_ROUTE_LARGE == kPathLarge && BSJ_ROUTE_DIRECT == kPathDirect && BSJ_ROUTE_BUCKET == kPathBucket &&
+              BSJ_ROUTE_RADIX == kPathRadix && BSJ_ROUTE_DENSE == kPathDense &&
+              BSJ_ROUTE_RANK_LSD == kPathRankLsd && BSJ_ROUTE_RAW_LSD == kPathRawLsd &&
+              BSJ_ROUTE_BITONIC == kPathBitonic, "route bits of bsj.h and the kernels differ");
+
+bsj_status bsj_plan_set_select_route(bsj_plan* p, int32_t flags)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    if ((flags & ~kSelAll) != 0 || ((flags & kSelForceLarge) && (flags & kSelNoLarge)))
+        return fail(p->ctx, BSJ_ERR_INVALID, "unknown or contradictory select route flags");
+    if (flags == p->select_force) return BSJ_OK;
+    // the flags are a launch argument baked into the captured graphs: capture again
+    cudaSetDevice(p->ctx->device);
+    for (auto& gv : p->graph)
+        for (cudaGraphExec_t& g : gv)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    p->select_force = flags;
     return BSJ_OK;
 }
 
-int32_t bsj_plan_chunk(const bsj_plan* p) { return (p && p->variant > 0) ? kChunkSizes[p->variant - 1] : 0; }
+bsj_status bsj_plan_select_routes(bsj_plan* p, uint32_t* routes)
+{
+    if (!p || !routes) return BSJ_ERR_INVALID;
+    bsj_context* ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    BSJ_CUDA(ctx, cudaStreamSynchronize(p->last_stream ? p->last_stream : ctx->stream));
+    std::vector<SegState> st(p->nseg);
+    BSJ_CUDA(ctx, cudaMemcpy(st.data(), p->d_state, sizeof(SegState) * p->nseg, cudaMemcpyDeviceToHost));
+    uint32_t r = 0;
+    for (const SegState& x : st) r |= x.select_paths;
+    *routes = r;
+    return BSJ_OK;
+}
+
+int32_t bsj_plan_chunk(const bsj_plan* p) { return (p && p->variant > 0) ? kStepVariantCode[p->variant - 1] : 0; }
 
 bsj_status bsj_plan_autotune(bsj_plan* p, void* stream, int32_t repeats, int32_t* chunk, float* ms)
 {
@@ -1036,7 +1090,7 @@ bsj_status bsj_plan_autotune(bsj_plan* p, void* stream, int32_t repeats, int32_t
     if (e != cudaSuccess) st = cuda_fail(ctx, e, "autotune events");
     float best = 0.f;
     int bv = -1;
-    for (int v = 0; v <= kNumChunkSizes && st == BSJ_OK; v++) {
+    for (int v = 0; v <= kNumStepVariants && st == BSJ_OK; v++) {
         if (ms) ms[v] = -1.f;
         if (v > 0 && v - 1 == rule_uniform) {
             if (ms) ms[v] = ms[0];

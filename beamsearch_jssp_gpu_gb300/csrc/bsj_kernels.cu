@@ -547,6 +547,345 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a,
 }
 
 // ------------------------------------------------------------------------------------
+// k_step_t: materialise + expand with one THREAD per survivor (gpu-v2 / clean beams).
+//
+// The warp-per-survivor k_step spreads one survivor's ready list over the lanes, so most
+// lanes idle (a 50-job ready list is two lane-rounds, the pivot machine's candidates a
+// handful of lanes) and one survivor costs ~800 warp instructions.  Here a warp takes 32
+// consecutive ranks (one 32-rank key chunk), each lane one survivor end to end: load the
+// parent snapshot, apply the selected op, store the child, scan the child's ready list
+// for the pivot machine's ops, score them and emit the keys in slot order (a warp scan
+// of the per-lane key counts).  No block-wide barrier: the warps of a CTA are independent.
+//
+// Staging of the parent snapshot in shared memory, chosen per plan (StepArgs::thread_step):
+//   1  16-byte global loads, batched, stored word-interleaved by lane (word x of lane l at
+//      [x*32 + l]): every per-thread access of any field is bank-conflict free;
+//   2  one cp.async.bulk (TMA bulk copy, global -> shared, completion on a per-warp
+//      mbarrier) per lane, the snapshot kept contiguous (16-byte-aligned rows: 4-way bank
+//      conflicts on field access).
+// Result-identical to k_step (the same arithmetic in the same order per child).
+// ------------------------------------------------------------------------------------
+constexpr int kTStepWarps = kTStepWarpsPerCta;  // warps (32-rank chunks) per CTA
+constexpr uint32_t kTSpinLimit = 1u << 22;     // mbarrier try_wait attempts before giving up
+
+__host__ __device__ __forceinline__ size_t tstep_smem_bytes(int sb_max, int max_n)
+{
+    return (size_t)kTStepWarps * 32 * ((size_t)sb_max + (size_t)max_n);
+}
+
+// One lane's snapshot in shared memory: word x at w[x * XS].
+template <int XS>
+struct TSnap {
+    uint32_t* w;
+    __device__ __forceinline__ uint32_t word(int x) const { return w[x * XS]; }
+    __device__ __forceinline__ void set_word(int x, uint32_t v) const { w[x * XS] = v; }
+    __device__ __forceinline__ int byte(int off) const { return (int)((w[(off >> 2) * XS] >> ((off & 3) * 8)) & 0xFFu); }
+    __device__ __forceinline__ void set_byte(int off, int v) const
+    {
+        reinterpret_cast<uint8_t*>(w + (off >> 2) * XS)[off & 3] = (uint8_t)v;
+    }
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <int XS>
+__device__ __forceinline__ void tsnap_load(const TSnap<XS>& S, const uint8_t* src, int w16)
+{
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    int q = 0;
+    for (; q + 4 <= w16; q += 4) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = __ldg(s4 + q + u);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            S.set_word(4 * (q + u) + 0, v[u].x);
+            S.set_word(4 * (q + u) + 1, v[u].y);
+            S.set_word(4 * (q + u) + 2, v[u].z);
+            S.set_word(4 * (q + u) + 3, v[u].w);
+        }
+    }
+    for (; q < w16; q++) {
+        const uint4 v = __ldg(s4 + q);
+        S.set_word(4 * q + 0, v.x);
+        S.set_word(4 * q + 1, v.y);
+        S.set_word(4 * q + 2, v.z);
+        S.set_word(4 * q + 3, v.w);
+    }
+}
+
+template <int XS>
+__device__ __forceinline__ void tsnap_store(const TSnap<XS>& S, uint8_t* dst, int w16)
+{
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int q = 0; q < w16; q++)
+        d4[q] = make_uint4(S.word(4 * q), S.word(4 * q + 1), S.word(4 * q + 2), S.word(4 * q + 3));
+}
+
+// Job-predecessor finish (pred_finish above, on a lane's snapshot).
+template <int XS>
+__device__ __forceinline__ int tpred_finish(const TSnap<XS>& S, const SegDesc& d, int j, int k)
+{
+    if (d.m == 1) return j > 0 ? (int)S.word((d.off_jr >> 2) + j - 1) : 0;
+    return k == 0 ? 0 : (int)S.word((d.off_jr >> 2) + j);
+}
+
+// Ready position of the b-th candidate of the expansion of this (parent) snapshot at
+// level t as rank c -- the pivot machine's ready ops in ready-list order -- or -1 when the
+// parent has at most b candidates.  Only filler ranks need it (a scored child's position
+// comes from the table its parent's expansion wrote).
+template <int XS>
+__device__ int tnth_candidate(const TSnap<XS>& S, const SegDesc& d, const uint32_t* ops, uint32_t seed_t,
+                              int c, int b)
+{
+    const int rr = (int)(S.word(d.off_hdr >> 2) & 0xFFFFu);
+    if (rr <= 0) return -1;
+    const uint32_t h = pivot_hash(seed_t + (uint32_t)c);
+    const int jp = S.byte(d.off_rd + (int)(h % (uint32_t)rr));
+    const int pm = (int)(__ldg(ops + d.op_off + jp * d.m + S.byte(d.off_nx + jp)) & 0xFFu);
+    int cnt = 0;
+    for (int i = 0; i < rr; i++) {
+        const int j = S.byte(d.off_rd + i);
+        if ((int)(__ldg(ops + d.op_off + j * d.m + S.byte(d.off_nx + j)) & 0xFFu) == pm) {
+            if (cnt == b) return i;
+            cnt++;
+        }
+    }
+    return -1;
+}
+
+template <int MODE_T>
+__global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
+{
+    constexpr bool BULK = (MODE_T == 2);
+    constexpr int XS = BULK ? 1 : 32;
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ __align__(8) unsigned long long s_mbar[kTStepWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sw = a.sb_max >> 2;   // words per snapshot slot
+    uint32_t* wbase = reinterpret_cast<uint32_t*>(smem) + (size_t)warp * 32 * sw;
+    TSnap<XS> S;
+    S.w = BULK ? wbase + (size_t)lane * sw : wbase + lane;
+    // candidate positions of this lane's expansion: entry b at posl[b * 32]
+    uint8_t* posl = smem + (size_t)kTStepWarps * 32 * a.sb_max + (size_t)warp * 32 * a.max_n + lane;
+    pdl_trigger();
+    if (BULK) {
+        if (lane == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&s_mbar[warp])), "r"(32) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncwarp();
+    }
+    uint32_t phase = 0;
+    pdl_wait();
+    for (int chunk = a.chunk_lo + blockIdx.x * kTStepWarps + warp; chunk < a.chunk_hi;
+         chunk += gridDim.x * kTStepWarps) {
+        const int seg = find_seg(a.chunk_prefix, a.seg_lo, a.seg_hi, chunk);
+        const SegDesc& d = a.segs[seg];
+        if (s >= d.N - 1) continue;   // the same for the whole warp (one chunk)
+        SegState& st = a.st[seg];
+        if (d.mode != MODE_V2 && d.mode != MODE_CLEAN) {   // the host runs only these beams here
+            if (lane == 0) atomicOr(&st.status, kStatusBadSelect);
+            continue;
+        }
+        const int q = chunk - __ldg(a.chunk_prefix + seg);
+        const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
+        const int n = d.n, m = d.m, w16 = d.sbytes >> 4;
+        const int r = q * 32 + lane;
+        const bool act = r < P;
+        uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
+        const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
+        const int hw = d.off_hdr >> 2;
+
+        // ---- 1. the source snapshot of this rank
+        uint32_t e = 0;
+        int c = 0, b = 0, ii = -1;
+        if (act && s >= 0) {
+            e = __ldg(a.sel + d.sel_off + r);
+            const uint32_t slot = e & ~kFillerFlag;
+            c = (int)(slot / (uint32_t)n);
+            b = (int)slot - c * n;
+        }
+        if (BULK) {
+            const uint32_t bar = smem_u32(&s_mbar[warp]);
+            if (act && s >= 0) {
+                // the slot was last written through the generic proxy: order that before
+                // the bulk copy's (async-proxy) write
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
+                             ::"r"(bar), "r"(d.sbytes) : "memory");
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                             ::"r"(smem_u32(S.w)), "l"(parent + (int64_t)c * d.sbytes), "r"(d.sbytes), "r"(bar)
+                             : "memory");
+            } else {
+                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar)
+                             : "memory");
+            }
+            if (act && s >= 0 && !(e & kFillerFlag)) ii = __ldg(a.pos_pool + d.pos_off[s & 1] + (e & ~kFillerFlag));
+            uint32_t done = 0;
+            for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
+                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                             " selp.u32 %0, 1, 0, p;\n}\n"
+                             : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+            }
+            phase ^= 1u;
+            if (!__all_sync(FULL_MASK, done)) {
+                // a copy that never completed: flag it, wait once more (bounded) for the
+                // warp's copies, and stop working on this launch
+                if (lane == 0) atomicOr(&st.status, kStatusBadSelect);
+                for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
+                    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                                 " selp.u32 %0, 1, 0, p;\n}\n"
+                                 : "=r"(done) : "r"(bar), "r"(phase ^ 1u) : "memory");
+                }
+                return;
+            }
+        } else {
+            if (act && s >= 0) {
+                if (!(e & kFillerFlag)) ii = __ldg(a.pos_pool + d.pos_off[s & 1] + (e & ~kFillerFlag));
+                tsnap_load<XS>(S, parent + (int64_t)c * d.sbytes, w16);
+            }
+        }
+
+        // ---- 2. materialise (v2: kernel_materialize_topk, gpu/v2_twophases/solver.cu:193-252)
+        uint32_t hist_val = kMark;
+        if (act && s < 0) {
+            for (int x = 0; x < (d.sbytes >> 2); x++) S.set_word(x, 0u);
+            for (int j = 0; j < n; j++) S.set_byte(d.off_rd + j, j);
+            S.set_word(hw, (uint32_t)n);
+            S.set_word(hw + 2, kMark);
+            tsnap_store<XS>(S, childbuf, w16);
+        } else if (act) {
+            if (e & kFillerFlag) ii = tnth_candidate<XS>(S, d, a.ops, d.seed + (uint32_t)s, c, b);
+            if (ii >= 0) {
+                const uint32_t h0 = S.word(hw);
+                const int r0 = (int)(h0 & 0xFFFFu), ns = (int)(h0 >> 16);
+                const int j = S.byte(d.off_rd + ii);
+                const int k = S.byte(d.off_nx + j);
+                const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
+                const int mc = (int)(o & 0xFFu);
+                const int pred = tpred_finish<XS>(S, d, j, k);
+                const int trv = (int)S.word(mc);
+                const int fin = (trv > pred ? trv : pred) + (int)(o >> 8);
+                const int lastj = S.byte(d.off_rd + r0 - 1);
+                const bool cont = (k + 1 < m);
+                const int cm = (int)S.word(hw + 1);
+                S.set_word(mc, (uint32_t)fin);
+                S.set_word((d.off_jr >> 2) + j, (uint32_t)fin);
+                if (ii != r0 - 1) S.set_byte(d.off_rd + ii, lastj);
+                if (cont) S.set_byte(d.off_rd + r0 - 1, j);
+                S.set_byte(d.off_nx + j, k + 1);
+                S.set_word(hw, ((uint32_t)(ns + 1) << 16) | (uint32_t)(r0 - 1 + (cont ? 1 : 0)));
+                S.set_word(hw + 1, (uint32_t)(cm > fin ? cm : fin));
+                hist_val = ((uint32_t)c << 8) | (uint32_t)j;
+                S.set_word(hw + 2, hist_val);
+                S.set_word(hw + 3, (uint32_t)(s + 1));
+                tsnap_store<XS>(S, childbuf + (int64_t)r * d.sbytes, w16);
+            } else {
+                // filler rank whose branch does not exist: v2 leaves the ping-pong slot as
+                // it was (gpu/v2_twophases/solver.cu:191) and expands what it holds
+                if (d.mode == MODE_CLEAN) atomicOr(&st.status, kStatusBadSelect);
+                tsnap_load<XS>(S, childbuf + (int64_t)r * d.sbytes, w16);
+            }
+            a.hist[d.hist_off + (int64_t)s * d.K + r] = hist_val;
+        }
+
+        // ---- 3. expand for level t (kernel_score_candidates, gpu/v2_twophases/solver.cu:68-123)
+        const int t = s + 1;
+        const uint32_t seed_t = d.seed + (uint32_t)t;
+        const bool lastlv = (t == d.N - 1);
+        int cnt = 0, pm = -1, trp = 0, pcmax = 0, ns1 = 1;
+        uint32_t vm0 = 0u, vm1 = 0u, vm2 = 0u, vm3 = 0u;
+        const int rr = act ? (int)(S.word(hw) & 0xFFFFu) : 0;
+        const int bound = st.bound;
+        if (rr > 0) {
+            const uint32_t h0 = S.word(hw);
+            ns1 = (int)(h0 >> 16) + 1;
+            pcmax = (int)S.word(hw + 1);
+            const uint32_t h = pivot_hash(seed_t + (uint32_t)r);
+            const int jp = S.byte(d.off_rd + (int)(h % (uint32_t)rr));
+            pm = (int)(__ldg(a.ops + d.op_off + jp * m + S.byte(d.off_nx + jp)) & 0xFFu);
+            trp = (int)S.word(pm);
+            uint8_t* prow = a.pos_pool + d.pos_off[t & 1] + (int64_t)r * n;
+            const bool rows = t < d.N - 1;
+            for (int i0 = 0; i0 < rr; i0 += 4) {
+                // off_rd = 4m + 4n is a multiple of 4: ready positions i0..i0+3 share a word
+                const uint32_t w4 = S.word((d.off_rd + i0) >> 2);
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int i = i0 + u;
+                    if (i < rr) {
+                        const int j = (int)((w4 >> (8 * u)) & 0xFFu);
+                        const int k = S.byte(d.off_nx + j);
+                        const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
+                        if ((int)(o & 0xFFu) == pm) {
+                            const int pred = tpred_finish<XS>(S, d, j, k);
+                            const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
+                            const int cmx = pcmax > fin ? pcmax : fin;
+                            if (cmx < bound) {   // gpu/v1/solver.cu:120
+                                const uint32_t bit = 1u << (cnt & 31);
+                                const int wq = cnt >> 5;
+                                vm0 |= (wq == 0) ? bit : 0u;
+                                vm1 |= (wq == 1) ? bit : 0u;
+                                vm2 |= (wq == 2) ? bit : 0u;
+                                vm3 |= (wq == 3) ? bit : 0u;
+                            }
+                            posl[cnt * 32] = (uint8_t)i;
+                            if (rows) prow[cnt] = (uint8_t)i;
+                            cnt++;
+                        }
+                    }
+                }
+            }
+        }
+        const int nv = __popc(vm0) + __popc(vm1) + __popc(vm2) + __popc(vm3);
+        // slot order inside the chunk: ranks ascending, branches ascending
+        int pre = nv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, pre, o);
+            if (lane >= o) pre += y;
+        }
+        const int total = __shfl_sync(FULL_MASK, pre, 31);
+        pre -= nv;
+        if (act) {
+#pragma unroll
+            for (int w = 0; w < 4; w++)
+                if (w < d.words)
+                    a.masks[d.mask_off + (int64_t)r * d.words + w] = w == 0 ? vm0 : (w == 1 ? vm1 : (w == 2 ? vm2 : vm3));
+        }
+        if (nv > 0) {
+            unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * 32 * n + pre;
+            const float fns = __int2float_rn(ns1);
+            int o_k = 0;
+            for (int bb = 0; bb < cnt; bb++) {
+                const uint32_t vw = (bb >> 5) == 0 ? vm0 : ((bb >> 5) == 1 ? vm1 : ((bb >> 5) == 2 ? vm2 : vm3));
+                if (!((vw >> (bb & 31)) & 1u)) continue;
+                const int i = posl[bb * 32];
+                const int j = S.byte(d.off_rd + i);
+                const int k = S.byte(d.off_nx + j);
+                const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
+                const int pred = tpred_finish<XS>(S, d, j, k);
+                const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
+                const int cmx = pcmax > fin ? pcmax : fin;
+                const float base = __fdiv_rn(__int2float_rn(cmx), fns);
+                const uint32_t ni = noise_hash(seed_t, (uint32_t)r, (uint32_t)bb) % 1000u;
+                const float sc = __fadd_rn(base, __ldg(a.noise + ni));
+                const uint32_t slot = (uint32_t)(r * n + bb);
+                kdst[o_k++] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
+                if (lastlv && ns1 == d.N) {
+                    atomicMin(&st.best, ((unsigned long long)(uint32_t)cmx << 32) |
+                                            ((unsigned long long)slot << 8) | (uint32_t)j);
+                    atomicMin(a.group_best + d.group, cmx);
+                }
+            }
+        }
+        if (lane == 0) a.kcnt[d.kcnt_off + q] = total;
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // k_select: exact top-K + stable order per beam (gpu modes).
 //
 // The reference sorts all P*n (score, slot) pairs with a stable radix sort and keeps the
@@ -1618,10 +1957,14 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
     const int R = V < keff ? V : keff;
     uint32_t* sel = a.sel + d.sel_off;
     const SelSmem S = sel_smem(smem);
+    const int fz = a.select_force;    // route flags (0 = by level size); uniform over the block
+    // routes taken, recorded by thread 0 with a reduction that returns nothing
+    auto route = [&](uint32_t bit) { if (tid == 0) atomicOr(&st.select_paths, bit); };
     // staged (shared-memory) input when the level fits; larger levels take select_large
     const bool staged = (V <= kStageKeys) && (K <= kLsdMax);
-    if (R > 0 && !staged && select_large(st, R, ks, sel, S)) {
-        // done: survivors 0..R-1 written
+    const bool try_large = (fz & kSelForceLarge) ? true : ((fz & kSelNoLarge) ? false : !staged);
+    if (R > 0 && try_large && select_large(st, R, ks, sel, S)) {
+        route(kPathLarge);   // done: survivors 0..R-1 written
     } else if (R > 0) {
         if (staged) stage_keys(ks, S.stg);
         const unsigned long long* stg = S.stg;
@@ -1631,17 +1974,21 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
         unsigned long long* dst = S.A;
         const int T = S.misc[2], shift = S.misc[4];
         const uint32_t smin = (uint32_t)S.misc[1];
-        const bool bucketed = count <= kLsdMax;   // survivors = the keys of buckets <= T
+        // survivors = the keys of buckets <= T
+        const bool bucketed = count <= kLsdMax && !(fz & kSelForceRadix);
         __syncthreads();
-        const bool direct = staged && V <= kDirectMaxKeys && count >= R &&
-                            select_direct(S.stg, V, R, T, shift, smin, sel, S);
+        const bool direct = !(fz & (kSelNoDirect | kSelForceRadix)) && staged && V <= kDirectMaxKeys &&
+                            count >= R && select_direct(S.stg, V, R, T, shift, smin, sel, S);
+        if (direct) route(kPathDirect);
         if (!direct) {
             if (bucketed) {
+                route(kPathBucket);
                 const uint32_t lim = ((uint32_t)T + 1u) << shift;  // bucket <= T
                 auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
                 count = staged ? compact_stable(get_s, V, keep, dst, kLsdMax, S)
                                : compact_stable(get_g, V, keep, dst, kLsdMax, S);
             } else {
+                route(kPathRadix);
                 if (tid == 0) st.select_fallbacks += 1;
                 unsigned long long pmask, prefix;
                 if (staged) radix_threshold(get_s, V, R, S, pmask, prefix);
@@ -1657,11 +2004,11 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
                 count = count > kStageKeys ? kStageKeys : count;
             }
             const int RR = R < count ? R : count;
-            if (count <= kLsdMax) {
+            if (count <= kLsdMax && !(fz & kSelBitonic)) {
                 const int E = (count + kSelectThreads - 1) / kSelectThreads;
                 int nd = -1;
                 DenseTables D;
-                if (bucketed) {
+                if (bucketed && !(fz & kSelNoDense)) {
                     // bucket counts are intact on the bucketed path (the radix path reuses them)
                     D.occ = reinterpret_cast<uint16_t*>(S.stg + kDenseOccOff);
                     D.bm = reinterpret_cast<uint32_t*>(S.stg + kDenseBmOff);
@@ -1671,16 +2018,21 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
                     };
                     nd = dense_build(each, T, shift, smin, S, D);
                 }
-                if (nd >= 0 && nd <= 256) {
+                if (nd >= 0 && nd <= 256 && !(fz & kSelRankLsd)) {
+                    route(kPathDense);
                     dense_sort_emit(dst, count, RR, D, sel, S);
                 } else {
-                    if (nd > 256) {
-                        // more distinct scores than one 8-bit pass: ranks into the keys, LSD passes
+                    if (nd >= 0) {
+                        // more distinct scores than one 8-bit pass (or the route is forced):
+                        // ranks into the keys, then LSD passes over the rank bits
+                        route(kPathRankLsd);
                         for (int i = tid; i < count; i += kSelectThreads) {
                             const unsigned long long k = dst[i];
                             dst[i] = ((unsigned long long)D.rank_of((uint32_t)(k >> 32)) << 32) | (k & 0xFFFFFFFFull);
                         }
                         __syncthreads();
+                    } else {
+                        route(kPathRawLsd);
                     }
                     unsigned long long* B = S.stg;
                     switch (E) {
@@ -1696,6 +2048,12 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
                     }
                 }
             } else {
+                route(kPathBitonic);
+                if (dst != S.stg) {
+                    // survivors in A (count <= kLsdMax): the bitonic sort works in stg
+                    for (int i = tid; i < count; i += kSelectThreads) S.stg[i] = dst[i];
+                    __syncthreads();
+                }
                 sort_and_emit(S.stg, count, RR, sel);
             }
         }
@@ -2310,6 +2668,14 @@ static cudaError_t for_each_step(F&& f)
     return e;
 }
 
+template <typename F>
+static cudaError_t for_each_tstep(F&& f)
+{
+    cudaError_t e = f(k_step_t<1>);
+    if (e == cudaSuccess) e = f(k_step_t<2>);
+    return e;
+}
+
 int nq_class(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
 
 // All level kernels run back to back; giving them one shared-memory carveout (the
@@ -2321,6 +2687,8 @@ static cudaError_t set_carveout()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
+    if (e == cudaSuccess)
+        e = for_each_tstep([&](auto fn) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gather_v1, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     return e;
@@ -2349,6 +2717,7 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
+    if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
     return e;
 }
 
@@ -2358,6 +2727,7 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
+    if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
     return e;
 }
 
@@ -2400,6 +2770,14 @@ static cudaError_t launch_step_ch(const StepArgs& a, int s, int grid, int nq_mas
 
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
+    if (a.thread_step) {
+        if (a.chunk != 32) return cudaErrorInvalidValue;
+        const size_t sm = tstep_smem_bytes(a.sb_max, a.max_n);
+        const int block = kTStepWarps * 32;
+        if (a.thread_step == 1) return launch_kernel(k_step_t<1>, grid, block, sm, stream, s >= 0, a, s);
+        if (a.thread_step == 2) return launch_kernel(k_step_t<2>, grid, block, sm, stream, s >= 0, a, s);
+        return cudaErrorInvalidValue;
+    }
     switch (a.chunk) {
     case 8: return launch_step_ch<8>(a, s, grid, nq_mask, stream);
     case 16: return launch_step_ch<16>(a, s, grid, nq_mask, stream);

@@ -26,6 +26,9 @@ struct StepArgs {
     int32_t chunk_lo, chunk_hi;
     int32_t rank_lo, rank_hi;
     int32_t chunk;                // ranks per k_step CTA (one of kChunkSizes)
+    int32_t select_force;         // kSel* route flags for k_select (0 = by level size)
+    int32_t thread_step;          // k_step form: 0 warp per survivor; 1 / 2 thread per survivor
+                                  // (k_step_t, chunk 32) with load / bulk-copy staging
     uint8_t* beam_pool;
     uint8_t* slot_pool;
     unsigned long long* keys;
@@ -40,6 +43,17 @@ struct StepArgs {
     const float* noise;           // [1000]: (float)k / 1e9f, IEEE round-to-nearest
     const double* dnoise;         // [1000]: (double)k / 1e6 (BS-PMS noise), IEEE round-to-nearest
 };
+
+// k_step variants (the autotuner's candidates besides the default rule): warp per
+// survivor with 8, 16 or 32 survivors per CTA; one thread per survivor (32 per warp, key
+// chunks of 32) with the parent snapshots staged by 16-byte loads or by bulk copies.
+// Thread variants apply to beam groups whose beams are all gpu-v2 / clean; other groups
+// run the warp kernel with 32 per CTA.  Public codes (bsj_plan_set_chunk): 8, 16, 32, 1, 2.
+constexpr int kNumStepVariants = 5;
+constexpr int kStepVariantChunk[kNumStepVariants] = {8, 16, 32, 32, 32};
+constexpr int kStepVariantThread[kNumStepVariants] = {0, 0, 0, 1, 2};
+constexpr int kStepVariantCode[kNumStepVariants] = {8, 16, 32, 1, 2};
+constexpr int kTStepWarpsPerCta = 4;   // k_step_t: warps (32-survivor chunks) per CTA
 
 // k_heap launch configuration: the largest K, child-table row (bytes) and n of the
 // launch's ICH/PMS beams, and the parents prepared per chunk.

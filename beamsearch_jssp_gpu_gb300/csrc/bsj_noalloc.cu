@@ -19,7 +19,9 @@
 // array and must be serialised by the caller.
 //
 // The kernels are the library's ordinary level kernels (k_step, k_select, k_finalize);
-// only the buffers they are handed differ.
+// only the buffers they are handed differ.  The per-call initial values reach the scratch
+// as kernel parameters, not as copies from host memory, so a call only enqueues work on
+// its stream and returns.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -60,7 +62,9 @@ cudaError_t scratch_address(void** out)
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // (duration << 8) | machine per op; an invalid entry is replaced by machine 0 / duration 0
-// (so no kernel indexes outside the instance) and flags the beam state.
+// (so no kernel indexes outside the instance) and flags the beam state.  Durations whose
+// sum reaches 2^31-1 would wrap the int32 makespans, so then the whole table is zeroed
+// and the state flagged the same way.
 __global__ void k_noalloc_pack(const int32_t* machine, const int32_t* duration, int count, int m,
                                uint32_t* ops, SegState* st)
 {
@@ -81,18 +85,42 @@ __global__ void k_noalloc_pack(const int32_t* machine, const int32_t* duration, 
     }
     atomicAdd(&total, local);
     __syncthreads();
-    if (bad || (threadIdx.x == 0 && total >= 0x7FFFFFFFull)) atomicOr(&st->status, 4);
+    const bool overflow = total >= 0x7FFFFFFFull;
+    if (overflow)
+        for (int q = threadIdx.x; q < count; q += blockDim.x) ops[q] = 0u;
+    if (bad || (threadIdx.x == 0 && overflow)) atomicOr(&st->status, 4);
 }
 
-// Result into the caller's buffer: [0] makespan (-1 if the instance was invalid),
-// [1] found, [2 .. 2+N) sequence.
+// Per-call initial values of the beam's descriptor, state, prefixes and bound, written
+// from kernel parameters (no host buffer is read, so nothing waits for the host).
+__global__ void k_noalloc_init(SegDesc d, SegState st, int32_t beam_width, int32_t nch, int32_t group,
+                               SegDesc* d_seg, SegState* d_st, int32_t* prefix, int32_t* cprefix,
+                               int32_t* d_group)
+{
+    if (threadIdx.x == 0) {
+        *d_seg = d;
+        *d_st = st;
+        prefix[0] = 0;
+        prefix[1] = beam_width;
+        cprefix[0] = 0;
+        cprefix[1] = nch;
+        *d_group = group;
+    }
+}
+
+// Result into the caller's buffer: [0] makespan (-1 if the instance was invalid, -2 if a
+// device consistency check of the level kernels failed), [1] found, [2 .. 2+N) sequence
+// (zeros unless [0] >= 0).
 __global__ void k_noalloc_out(const SegState* st, const int32_t* seq, int N, int32_t* out)
 {
-    const bool invalid = (st->status & 4) != 0;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) out[2 + t] = invalid ? 0 : seq[t];
+    const int status = st->status;
+    const bool invalid = (status & 4) != 0;
+    const bool corrupt = (status & (kStatusBadLineage | kStatusBadSelect)) != 0;
+    const bool ok = !invalid && !corrupt;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) out[2 + t] = ok ? seq[t] : 0;
     if (threadIdx.x == 0) {
-        out[0] = invalid ? -1 : st->makespan;
-        out[1] = invalid ? 0 : st->found;
+        out[0] = invalid ? -1 : (corrupt ? -2 : st->makespan);
+        out[1] = ok ? st->found : 0;
     }
 }
 
@@ -159,9 +187,6 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     st.bound = best_known;
     st.best = ~0ull;
     st.best_cmax = kSentinel;
-    const int32_t prefix[2] = {0, beam_width};
-    const int32_t cprefix[2] = {0, nch};
-    const int32_t group = best_known;
 
     StepArgs a{};
     a.segs = reinterpret_cast<const SegDesc*>(base + o_seg);
@@ -204,13 +229,14 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     const int nq_mask = 1 << d.nq;
 
     // everything that must start at zero or at its initial value is rewritten here
-    cudaError_t e = cudaMemcpyAsync(base + o_seg, &d, sizeof(d), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_state, &st, sizeof(st), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_prefix, prefix, sizeof(prefix), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_cprefix, cprefix, sizeof(cprefix), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_group, &group, sizeof(group), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(base + o_beam, 0, 2 * align_up(K * d.sbytes, 256), s);
-    if (e != cudaSuccess) return BSJ_ERR_CUDA;
+    k_noalloc_init<<<1, 32, 0, s>>>(d, st, beam_width, nch, best_known,
+                                    reinterpret_cast<SegDesc*>(base + o_seg),
+                                    reinterpret_cast<SegState*>(base + o_state),
+                                    reinterpret_cast<int32_t*>(base + o_prefix),
+                                    reinterpret_cast<int32_t*>(base + o_cprefix),
+                                    reinterpret_cast<int32_t*>(base + o_group));
+    if (cudaGetLastError() != cudaSuccess) return BSJ_ERR_CUDA;
+    if (cudaMemsetAsync(base + o_beam, 0, 2 * align_up(K * d.sbytes, 256), s) != cudaSuccess) return BSJ_ERR_CUDA;
     k_noalloc_pack<<<1, 256, 0, s>>>(d_machine, d_duration, d.N, m, reinterpret_cast<uint32_t*>(base + o_ops),
                                      reinterpret_cast<SegState*>(base + o_state));
     if (cudaGetLastError() != cudaSuccess) return BSJ_ERR_CUDA;

@@ -12,7 +12,8 @@
 //   - finished plans go to an idle pool keyed by shape (n, m, K, mode) and the next
 //     request of that shape reuses the plan and its graph (bsj_plan_update: new data, no
 //     allocation, no re-capture); idle plans are freed, oldest first, when memory is short;
-//   - bsj_poll / bsj_wait hand out the result with the request's queue and run times.
+//   - bsj_poll / bsj_wait hand out the result with the request's queue and run times;
+//   - bsj_server_prepare queues plan builds of a shape before its requests arrive.
 // A request's result does not depend on what else runs: every plan owns its memory and
 // the kernels of one request read nothing of another's.
 #include <chrono>
@@ -48,6 +49,8 @@ struct Request {
     int64_t bytes = 0;  // device footprint of its plan
     std::string shape;
     Clock::time_point submitted, admitted;
+    bool prepare = false;  // bsj_server_prepare: build and pool a plan, no result
+    bool built = false;    // no idle plan was free: this request built its plan
 };
 
 struct Done {
@@ -132,7 +135,7 @@ void bsj_server::evict_idle(int64_t need)
 bool bsj_server::admit_one(Request& r, Slot& s)
 {
     bsj_instance inst{r.n, r.m, r.machine.data(), r.duration.data()};
-    bsj_plan* p = take_idle(r.shape);
+    bsj_plan* p = r.prepare ? nullptr : take_idle(r.shape);
     bsj_status st = BSJ_OK;
     const Clock::time_point t0 = Clock::now();
     const bool reused = (p != nullptr);
@@ -158,6 +161,10 @@ bool bsj_server::admit_one(Request& r, Slot& s)
             stats.build_ms += prep + run;
         }
     }
+    if (st != BSJ_OK && r.prepare) {
+        if (p) bsj_plan_destroy(p);
+        return false;
+    }
     if (st != BSJ_OK) {
         if (p) bsj_plan_destroy(p);
         Done d;
@@ -171,6 +178,7 @@ bool bsj_server::admit_one(Request& r, Slot& s)
     }
     s.plan = p;
     s.req = std::move(r);
+    s.req.built = !reused;
     s.busy = true;
     bytes_inflight += bsj_plan_device_bytes(p);
     return true;
@@ -187,6 +195,7 @@ void bsj_server::finish(Slot& s)
     const double collect = ms_between(now, Clock::now());
     d.times.queue_ms = ms_between(s.req.submitted, s.req.admitted);
     d.times.run_ms = ms_between(s.req.admitted, now);
+    d.times.built_plan = s.req.built ? 1 : 0;
     bytes_inflight -= bsj_plan_device_bytes(s.plan);
     if (d.status == BSJ_OK) {
         idle[s.req.shape].push_back(s.plan);
@@ -198,6 +207,11 @@ void bsj_server::finish(Slot& s)
     s.plan = nullptr;
     s.busy = false;
     std::lock_guard<std::mutex> lk(mu);
+    if (s.req.prepare) {
+        // a prepared plan: pooled above (counted once it is there), nobody waits for it
+        if (d.status == BSJ_OK) stats.plans_prepared++;
+        return;
+    }
     finished[s.req.ticket] = std::move(d);
     stats.completed++;
     stats.collect_ms += collect;
@@ -225,7 +239,7 @@ void bsj_server::run()
                 std::lock_guard<std::mutex> lk(mu);
                 if (stop || pending.empty()) break;
                 const Request& head = pending.front();
-                const bool reusable = idle.count(head.shape) && !idle[head.shape].empty();
+                const bool reusable = !head.prepare && idle.count(head.shape) && !idle[head.shape].empty();
                 // a request whose plan would exceed the budget waits for running ones,
                 // unless nothing runs (it was checked against the budget at submit)
                 if (!reusable && busy > 0 && bytes_inflight + head.bytes > budget) break;
@@ -316,9 +330,10 @@ void bsj_server_destroy(bsj_server* s)
     delete s;
 }
 
-bsj_status bsj_submit(bsj_server* s, const bsj_instance* inst, const bsj_beam* beam, uint64_t* ticket)
+static bsj_status intake(bsj_server* s, const bsj_instance* inst, const bsj_beam* beam, uint64_t* ticket,
+                         int32_t prepare_copies)
 {
-    if (!s || !inst || !beam || !ticket || !inst->machine || !inst->duration) return BSJ_ERR_INVALID;
+    if (!s || !inst || !beam || !inst->machine || !inst->duration) return BSJ_ERR_INVALID;
     if (inst->n < 1 || inst->m < 1 || inst->n > BSJ_MAX_JOBS || inst->m > BSJ_MAX_MACHINES ||
         (int64_t)inst->n * inst->m > BSJ_MAX_OPS)
         return BSJ_ERR_LIMIT;
@@ -339,15 +354,32 @@ bsj_status bsj_submit(bsj_server* s, const bsj_instance* inst, const bsj_beam* b
         bsj_status st = bsj_plan_estimate(s->est_ctx, 1, &view, 1, &r.beam, &r.bytes);
         if (st != BSJ_OK) return st;
         if (r.bytes > s->budget) return BSJ_ERR_LIMIT;
-        r.ticket = s->next_ticket++;
         r.submitted = Clock::now();
-        *ticket = r.ticket;
-        s->live[r.ticket] = 1;
-        s->stats.submitted++;
-        s->pending.push_back(std::move(r));
+        if (prepare_copies > 0) {
+            r.prepare = true;
+            for (int32_t k = 0; k < prepare_copies; k++) s->pending.push_back(r);
+        } else {
+            r.ticket = s->next_ticket++;
+            *ticket = r.ticket;
+            s->live[r.ticket] = 1;
+            s->stats.submitted++;
+            s->pending.push_back(std::move(r));
+        }
     }
     s->cv_work.notify_one();
     return BSJ_OK;
+}
+
+bsj_status bsj_submit(bsj_server* s, const bsj_instance* inst, const bsj_beam* beam, uint64_t* ticket)
+{
+    if (!ticket) return BSJ_ERR_INVALID;
+    return intake(s, inst, beam, ticket, 0);
+}
+
+bsj_status bsj_server_prepare(bsj_server* s, const bsj_instance* inst, const bsj_beam* beam, int32_t copies)
+{
+    if (copies < 1 || copies > 256) return BSJ_ERR_INVALID;
+    return intake(s, inst, beam, nullptr, copies);
 }
 
 static void hand_out(Done& d, bsj_result* result, bsj_request_times* times)

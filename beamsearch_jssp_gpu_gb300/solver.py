@@ -214,6 +214,21 @@ class Plan:
     def set_timing(self, on: bool):
         self.ctx._check(self.lib.bsj_plan_set_timing(self.h, 1 if on else 0))
 
+    def set_select_route(self, *flags: str):
+        """Force the gpu-mode levels' top-K selection onto routes (names of
+        ``_native.SELECT``: force_large, no_large, no_direct, radix, no_dense, rank_lsd,
+        bitonic); no names = the normal choice by level size (bsj_plan_set_select_route)."""
+        v = 0
+        for f in flags:
+            v |= nat.SELECT[f]
+        self.ctx._check(self.lib.bsj_plan_set_select_route(self.h, v))
+
+    def select_routes(self) -> set:
+        """Names (``_native.ROUTE``) of the selection routes the last run took."""
+        r = ctypes.c_uint32()
+        self.ctx._check(self.lib.bsj_plan_select_routes(self.h, ctypes.byref(r)))
+        return {k for k, bit in nat.ROUTE.items() if r.value & bit}
+
     def autotune(self, repeats: int = 2, stream: int = 0) -> dict:
         """Time every k_step chunk candidate on this plan and keep the fastest
         (bsj_plan_autotune).  Returns {"chunk": choice, "ms": {candidate: ms per run}},
@@ -299,7 +314,21 @@ class Server:
         d = _result_dict(res, seq)
         d["queue_ms"] = times.queue_ms
         d["run_ms"] = times.run_ms
+        d["built_plan"] = bool(times.built_plan)
         return d
+
+    def prepare(self, machine, duration, mode: str = "v2", beam_width: int = 1024, copies: int = 1,
+                seed: int = 0):
+        """Build ``copies`` plans of this request shape (n, m, mode, K) ahead of traffic
+        (bsj_server_prepare): later requests of the shape reuse them."""
+        mc = np.ascontiguousarray(machine, dtype=np.int32)
+        du = np.ascontiguousarray(duration, dtype=np.int32)
+        n, m = mc.shape
+        inst = nat.Instance(n, m, _i32p(mc), _i32p(du))
+        beam = BeamSpec(mode, beam_width, nat.NO_BOUND, seed).to_c()
+        st = self.lib.bsj_server_prepare(self.h, ctypes.byref(inst), ctypes.byref(beam), int(copies))
+        if st != nat.BSJ_OK:
+            raise nat.BsjError(st, "prepare rejected")
 
     def poll(self, ticket: int) -> Optional[dict]:
         seq = np.zeros(self._n.get(ticket, 1), dtype=np.int32)

@@ -11,11 +11,20 @@ one set of launches sharing a device best-makespan word.  Metric = scored childr
 Arms:
   (default)          libbsj.so on the GPU: ``value`` device-timed with the instance
                      resident, ``e2e`` through the C ABI from host buffers.
-  --impl reference   the reference's CPU implementation of machine-focused beam search
-                     (cpu/v1_pms/solver.cpp), as the oracle port pinned to it, one process
-                     per beam on the host cores, each step a bounded sample of levels.
+  --impl reference   the reference's own CPU implementation of machine-focused beam search,
+                     BS-PMS (cpu/v1_pms/solver.cpp: glibc rand() pivots, fp64 score,
+                     libstdc++ bounded heap), as the oracle port pinned bit for bit to it,
+                     one process per beam on the host cores, each step a full 1 000-level
+                     search of the 8 beams.  The reference has no CPU implementation of its
+                     gpu-v2 semantics; the same workload in those semantics on the host
+                     cores is the default arm's ``cpu_baseline`` (the matched comparison).
 
 Also on the JSON line (rank 0; --no-extras skips them):
+  "cpu_baseline"      the oracle's restatement of gpu/v2_twophases (the headline's own
+             algorithm) over the same 8 beams, all 1 000 levels, a process per beam;
+  "cpu_baseline_pms"  the BS-PMS port (what --impl reference times) on the same beams;
+  "matched_ratios"    GPU over CPU in the same semantics: value and e2e over cpu_baseline,
+             pms_exact over cpu_baseline_pms;
   "pms_exact" the same 8 beams in BS-PMS mode (the reference CPU solver's exact semantics,
              serial bounded heap per beam), candidates/s and makespans;
   "batched"  256 synthetic instances of uneven size (n in {10..100}, m in {5..20},
@@ -51,31 +60,38 @@ CPU_SAMPLE_LEVELS = 1000       # levels per beam in one CPU sample (a full 50x20
 L2_FLUSH_BYTES = 512 << 20     # > 129 MB L2
 
 
-def _config(world: int) -> dict:
-    return {"workload": f"BS-PMS pivot-machine beam search, gpu-v2 semantics, {N_JOBS}x{N_MACH} synthetic "
-                        f"(seed {INSTANCE_SEED}), K={K}, {BEAMS} seeded beams per GPU in one launch, all "
-                        f"{N_JOBS * N_MACH} levels",
-            "jobs": N_JOBS, "machines": N_MACH, "beam_width": K, "beams_per_gpu": BEAMS, "mode": MODE,
+def _config(world: int, mode: str = MODE) -> dict:
+    what = {"v2": "pivot-machine beam search, gpu/v2_twophases semantics (hashed pivot and noise, fp32 score, "
+                  "stable top-K sort)",
+            "pms": "BS-PMS, cpu/v1_pms semantics (glibc rand() pivot and noise, fp64 score, libstdc++ bounded "
+                   "heap)"}[mode]
+    return {"workload": f"{what}, {N_JOBS}x{N_MACH} synthetic (seed {INSTANCE_SEED}), K={K}, {BEAMS} seeded "
+                        f"beams per GPU, all {N_JOBS * N_MACH} levels",
+            "jobs": N_JOBS, "machines": N_MACH, "beam_width": K, "beams_per_gpu": BEAMS, "mode": mode,
             "levels": N_JOBS * N_MACH, "parallelism": f"replicas x{world}",
             "l2": "flushed between timed steps (512 MB write); per-level working set ~26 MB stays L2-resident "
                   "within a step"}
 
 
 # ------------------------------------------------------------------------------------
-# CPU side (oracle port of cpu/v1_pms/solver.cpp, pinned bit-for-bit to the reference)
+# CPU side: the oracle (pinned bit for bit to the reference) on the host cores
 # ------------------------------------------------------------------------------------
+CPU_KIND = {"v2": "oracle restatement of gpu/v2_twophases/solver.cu (the headline's semantics)",
+            "pms": "oracle port of cpu/v1_pms/solver.cpp (pinned to the reference)"}
+
+
 def _cpu_worker(args):
-    seed, levels = args
+    n, m, iseed, width, mode, seed, levels = args
     from beamsearch_jssp_gpu_gb300.instance import synthetic_instance
     from oracle import oracle as O
 
-    mc, du = synthetic_instance(N_JOBS, N_MACH, INSTANCE_SEED)
+    mc, du = synthetic_instance(n, m, iseed)
     t0 = time.perf_counter()
-    r = O.solve(mc, du, "pms", K, seed, max_levels=levels)
+    r = O.solve(mc, du, mode, width, seed, max_levels=levels)
     return r["expanded"], time.perf_counter() - t0
 
 
-def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS, pool=None) -> dict:
+def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS, pool=None, mode: str = "pms") -> dict:
     """One bounded sample on the host cores, a process per beam (`pool`: reuse an open
     spawn pool of `procs` workers)."""
     from oracle import oracle as O
@@ -83,13 +99,19 @@ def cpu_sample(procs: int, seeds, levels: int = CPU_SAMPLE_LEVELS, pool=None) ->
     if pool is None:
         O.build(ref=False)
         with mp.get_context("spawn").Pool(procs) as own:
-            return cpu_sample(procs, seeds, levels, own)
+            return cpu_sample(procs, seeds, levels, own, mode)
     t0 = time.perf_counter()
-    out = pool.map(_cpu_worker, [(s, levels) for s in seeds])
+    out = pool.map(_cpu_worker, [(N_JOBS, N_MACH, INSTANCE_SEED, K, mode, s, levels) for s in seeds])
     wall = time.perf_counter() - t0
     expanded = sum(e for e, _ in out)
     busy = max(t for _, t in out)
     return dict(expanded=expanded, wall=wall, busy=busy, value=expanded / busy)
+
+
+def cpu_baseline_entry(r: dict, procs: int, mode: str) -> dict:
+    return {"value": r["value"], "unit": UNIT, "cores": procs, "kind": "port", "mode": mode,
+            "sample": f"{CPU_KIND[mode]}: levels 0-{CPU_SAMPLE_LEVELS - 1} (whole searches) of {BEAMS} beams "
+                      f"(seeds 0-{BEAMS - 1}), one process per beam, {r['busy']:.1f} s"}
 
 
 def reference_arm(args) -> int:
@@ -99,10 +121,6 @@ def reference_arm(args) -> int:
         return 0
     procs = max(1, min(BEAMS, os.cpu_count() or 1))
     seeds = list(range(BEAMS))
-    # each step a bounded sample: ~10 000 levels of the 8 beams over the whole run (a full
-    # 1 000-level search per step at 10 steps), 100 to 1 000 levels per step, so any
-    # --steps finishes in about a minute and a half on the GPU host's cores
-    levels = max(100, min(CPU_SAMPLE_LEVELS, 10000 // max(1, args.steps)))
     from oracle import oracle as O
 
     O.build(ref=False)
@@ -110,17 +128,18 @@ def reference_arm(args) -> int:
     with mp.get_context("spawn").Pool(procs) as pool:
         for _ in range(args.warmup):
             cpu_sample(procs, seeds, levels=20, pool=pool)
+        # every step: whole 1 000-level searches of the 8 beams, whatever --steps is
         for _ in range(args.steps):
-            r = cpu_sample(procs, seeds, levels=levels, pool=pool)
+            r = cpu_sample(procs, seeds, levels=CPU_SAMPLE_LEVELS, pool=pool)
             vals.append(r["value"])
             times.append(r["busy"])
     value = sum(vals) / len(vals)
-    sample = (f"levels 0-{levels - 1} of each of {BEAMS} beams (seeds 0-{BEAMS - 1}), "
+    sample = (f"{CPU_KIND['pms']}: whole {CPU_SAMPLE_LEVELS}-level searches of {BEAMS} beams (seeds 0-{BEAMS - 1}), "
               f"{procs} processes, per step")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
-            "data": "synthetic", "config": _config(world),
+            "data": "synthetic", "config": _config(world, "pms"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -230,14 +249,16 @@ def gpu_arm(args) -> int:
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
 
-    cpu = None
+    cpu = cpu_pms = None
     if rank == 0 and not args.no_cpu_baseline:
         # oracle pool started (spawn) before this process touches the GPU
         procs = max(1, min(BEAMS, os.cpu_count() or 1))
-        r = cpu_sample(procs, list(range(BEAMS)))
-        cpu = {"value": r["value"], "unit": UNIT, "cores": procs, "kind": "port",
-               "sample": f"oracle port of cpu/v1_pms/solver.cpp (pinned to the reference), levels "
-                         f"0-{CPU_SAMPLE_LEVELS - 1} of {BEAMS} beams, {procs} processes, {r['busy']:.1f} s"}
+        from oracle import oracle as O
+
+        O.build(ref=False)
+        with mp.get_context("spawn").Pool(procs) as pool:
+            cpu = cpu_baseline_entry(cpu_sample(procs, list(range(BEAMS)), pool=pool, mode=MODE), procs, MODE)
+            cpu_pms = cpu_baseline_entry(cpu_sample(procs, list(range(BEAMS)), pool=pool, mode="pms"), procs, "pms")
 
     torch.cuda.set_device(local)
     from beamsearch_jssp_gpu_gb300 import BeamSpec, Context, synthetic_instance
@@ -330,6 +351,13 @@ def gpu_arm(args) -> int:
         extras["batched"] = batched_stream(ctx)
         extras["serving"] = served_stream(ctx, local)
 
+    if rank == 0 and cpu:
+        extras["cpu_baseline_pms"] = cpu_pms
+        matched = {"value_over_cpu_baseline": value / cpu["value"],
+                   "e2e_over_cpu_baseline": (expanded_all / e2e_t) / cpu["value"]}
+        if "pms_exact" in extras:
+            matched["pms_exact_over_cpu_baseline_pms"] = extras["pms_exact"]["expanded_per_s"] / cpu_pms["value"]
+        extras["matched_ratios"] = matched
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",

@@ -161,26 +161,62 @@ bsj_status bsj_plan_stats(const bsj_plan *plan, double *step_bytes, double *sele
 bsj_status bsj_plan_set_timing(bsj_plan *plan, int enable);
 bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches, int count);
 
+/* ---- Top-K selection routes (no counterpart in the reference, which sorts every slot
+   with cub::DeviceRadixSort::SortPairs, gpu/v1/solver.cu:255-258) ----
+   The selection kernel of the gpu modes (v1, v2, clean) picks a route per level by its
+   size: the direct staged pass, bucket compaction + dense-rank sort, and for rare or
+   large levels the radix-select, raw-LSD, rank-LSD, bitonic and large-level routes.  All
+   give the same stable (score, slot) order.  bsj_plan_set_select_route forces the plan's
+   levels onto routes (BSJ_SELECT_* flags OR'd; 0 = the normal choice), so every route
+   can be checked on small inputs; the plan's captured graphs are rebuilt on its next
+   run.  BSJ_SELECT_FORCE_LARGE and BSJ_SELECT_NO_LARGE exclude each other.
+   bsj_plan_select_routes: BSJ_ROUTE_* bits of the routes the last run took (OR over the
+   plan's beams and levels; waits for the run). */
+#define BSJ_SELECT_FORCE_LARGE 1  /* large-level route (keys read in place) at any size */
+#define BSJ_SELECT_NO_LARGE    2  /* never the large-level route */
+#define BSJ_SELECT_NO_DIRECT   4  /* compact the survivors first (no direct staged pass) */
+#define BSJ_SELECT_RADIX       8  /* MSD radix select of the K-th key (no bucket threshold) */
+#define BSJ_SELECT_NO_DENSE    16 /* LSD passes over the raw score bits */
+#define BSJ_SELECT_RANK_LSD    32 /* dense ranks written into the keys, then LSD passes */
+#define BSJ_SELECT_BITONIC     64 /* block bitonic sort of the survivors */
+#define BSJ_ROUTE_LARGE    1
+#define BSJ_ROUTE_DIRECT   2
+#define BSJ_ROUTE_BUCKET   4
+#define BSJ_ROUTE_RADIX    8
+#define BSJ_ROUTE_DENSE    16
+#define BSJ_ROUTE_RANK_LSD 32
+#define BSJ_ROUTE_RAW_LSD  64
+#define BSJ_ROUTE_BITONIC  128
+bsj_status bsj_plan_set_select_route(bsj_plan *plan, int32_t flags);
+bsj_status bsj_plan_select_routes(bsj_plan *plan, uint32_t *routes);
+
 /* ---- Autotuning (no counterpart in the reference, whose launch shape is fixed:
    one block of n threads per parent, gpu/v1/solver.cu:186,237) ----
-   The materialise+expand kernel works on chunks of consecutive survivors of one beam per
-   thread block: 8, 16 or 32 (1, 2 or 4 per warp).  Small chunks spread a narrow level
-   over more SMs, large ones amortise per-block work; which is faster depends on n, m, K
-   and the number of beams, and results never depend on it.  Each beam group of a plan
-   (a graph branch) has its own size.  Candidates ("chunk" values): 0 = the default rule
-   (per group, from the plan's survivors per level and the group's n), 8, 16, 32 = that
-   size for every group.
+   The materialise+expand kernel has five forms ("chunk" codes), and which is fastest
+   depends on n, m, K and the number of beams; results never depend on it:
+     8, 16, 32   a warp per survivor (the ready list spread over the lanes), 8, 16 or 32
+                 consecutive survivors per thread block: small chunks spread a narrow level
+                 over more SMs, large ones amortise per-block work;
+     1, 2        a thread per survivor, 32 consecutive survivors per warp (far fewer
+                 instructions per survivor; gpu-v2 / clean beams only -- other beams of
+                 the group run the 32-survivor warp form): the parent snapshots are
+                 staged in shared memory by 16-byte loads (1) or by bulk copies with an
+                 mbarrier (2).
+   Each beam group of a plan (a graph branch) has its own form.  Candidates: 0 = the
+   default rule (per group, from the plan's survivors per level, the group's n and
+   modes), and each code above for every group.
    bsj_plan_autotune runs the plan once per candidate (an untimed run that also captures
    its graph, then `repeats` timed runs on `stream`, synchronously), keeps the fastest,
    and records it in a process-wide table keyed by device and batch shape, so later plans
    of the same shape (any context, the server included) start with it.  ms (may be NULL)
-   receives the mean ms per run of each candidate in the order 0, 8, 16, 32 (a uniform
-   size equal to what the rule gives every group is not run again: its entry repeats the
-   rule's); *chunk (may be NULL) the choice.  The plan's results afterwards are those of
-   a complete run.  Plans start with the tuned candidate of their shape if there is one,
-   else the rule.  bsj_plan_set_chunk selects a candidate; bsj_plan_chunk returns it.
+   receives the mean ms per run of each candidate in the order 0, 8, 16, 32, 1, 2 (six
+   floats; a form equal to what the rule gives every group is not run again: its entry
+   repeats the rule's); *chunk (may be NULL) the choice.  The plan's results afterwards
+   are those of a complete run.  Plans start with the tuned candidate of their shape if
+   there is one, else the rule.  bsj_plan_set_chunk selects a candidate; bsj_plan_chunk
+   returns it.
    bsj_set_autotune: with enable != 0, bsj_solve_batch / bsj_solve tune every batch shape
-   they have not seen on this device before its first solve (about 4 extra solves once
+   they have not seen on this device before its first solve (about 6 extra solves once
    per shape). */
 bsj_status bsj_plan_autotune(bsj_plan *plan, void *stream, int32_t repeats, int32_t *chunk, float *ms);
 bsj_status bsj_plan_set_chunk(bsj_plan *plan, int32_t chunk);
@@ -221,6 +257,9 @@ typedef struct {
 typedef struct {
     double queue_ms;         /* submit -> admission */
     double run_ms;           /* admission -> completion seen by the server */
+    int32_t built_plan;      /* 1 if no idle plan of the request's shape was free and the
+                                server built one (allocation + graph capture on its run) */
+    int32_t reserved;
 } bsj_request_times;
 typedef struct {
     int64_t submitted, completed;
@@ -233,6 +272,8 @@ typedef struct {
        (allocation + graph capture on first run), loading requests into reused plans,
        launching, and collecting results */
     double build_ms, update_ms, launch_ms, collect_ms;
+    int64_t plans_prepared;  /* plans built by bsj_server_prepare and now in the idle pool
+                                (included in plans_built) */
 } bsj_server_stats;
 /* cfg may be NULL (defaults). */
 bsj_status bsj_server_create(bsj_server **out, int device, const bsj_server_config *cfg);
@@ -252,6 +293,15 @@ bsj_status bsj_poll(bsj_server *server, uint64_t ticket, bsj_result *result,
 bsj_status bsj_wait(bsj_server *server, uint64_t ticket, bsj_result *result,
                     bsj_request_times *times);
 bsj_status bsj_server_get_stats(bsj_server *server, bsj_server_stats *out);
+/* Builds `copies` plans of the shape of (inst, beam) -- n, m, mode, K -- ahead of the
+   requests that will need them: each is created, run once on `inst` (which captures its
+   graph) and kept in the idle pool, so requests of that shape arriving later reuse a
+   ready plan instead of building one while they wait.  Queued behind earlier requests
+   and handled by the worker like them, within the memory budget (idle plans remain
+   subject to eviction when memory is short); produces no result.  Errors as bsj_submit.
+   A long-running server calls it once per shape it expects, before traffic arrives. */
+bsj_status bsj_server_prepare(bsj_server *server, const bsj_instance *inst, const bsj_beam *beam,
+                              int32_t copies);
 
 /* Single-beam solve that allocates nothing (no counterpart in the reference).
    For callers that must not allocate device memory -- operator/plugin hosts whose device
@@ -261,10 +311,15 @@ bsj_status bsj_server_get_stats(bsj_server *server, bsj_server_stats *out);
    BSJ_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit.
      d_machine, d_duration  device [n*m] int32 (machines 0-based), read only
      mode                   BSJ_MODE_V2 or BSJ_MODE_CLEAN
-     d_out                  device [2 + n*m] int32: makespan (-1 if the instance holds a
-                            machine id outside [0,m) or a duration outside [0,2^24)),
-                            found, then the 1-based op sequence
-   Asynchronous on `stream` (a cudaStream_t, NULL = default stream).  Returns
+     d_out                  device [2 + n*m] int32: makespan, found, then the 1-based op
+                            sequence.  The makespan is -1 (found 0, sequence zeros) if
+                            the instance holds a machine id outside [0,m), a duration
+                            outside [0,2^24), or durations summing to 2^31-1 or more;
+                            it is -2 (found 0, sequence zeros) if a device consistency
+                            check of the level kernels failed (what bsj_solve reports
+                            as BSJ_ERR_DEVICE)
+   Asynchronous on `stream` (a cudaStream_t, NULL = default stream): the call only
+   enqueues kernels and a memset and reads no host memory on the stream.  Returns
    BSJ_ERR_LIMIT when n, m, beam_width exceed the BSJ_MAX_* limits or the beam's working
    set (about 2*K*(4m+6n+16) + 10*K*n + 4*K*n*m bytes) exceeds the scratch array.  The
    first call on each device looks up the scratch array's device address: make it before

@@ -19,7 +19,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_LIB = os.path.join(HERE, "_build", "liborc.so")
 REF_CPU_LIB = os.path.join(HERE, "_ref", "libref_cpu.so")
-REF_TREE = "/root/reference"
 
 MODES = {"v1": 0, "v2": 1, "clean": 2, "ich": 3, "pms": 4}
 MARK = 0xFFFFFFFF
@@ -60,13 +59,22 @@ class _Result(ctypes.Structure):
 
 
 def build(ref: Optional[bool] = None) -> None:
-    """Compile liborc.so; also the reference builds (``make ref``) when the reference
-    tree exists (``ref=None``) or when asked."""
+    """Compile liborc.so; also the reference's own solvers from their sources: with
+    ``ref=None`` when the reference tree exists (``make ref-if-present``; the tree's
+    location is the Makefile's, overridable by BSJ_REFERENCE_TREE), with ``ref=True``
+    always (``make ref``)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if ref is None:
-        ref = os.path.isdir(REF_TREE)
-    if ref:
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"])
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref-if-present"])
+    elif ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+
+
+def reference_tree() -> str:
+    """Location of the reference tree as the Makefile resolves it (BSJ_REFERENCE_TREE, else
+    the recipe's default); the tree may be absent."""
+    return subprocess.check_output(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                                   text=True).strip()
 
 
 _orc = None

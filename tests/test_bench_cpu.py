@@ -39,7 +39,7 @@ def test_config_names_the_workload():
     assert "workload" in c and "l2" in c
 
 
-def test_command_line_modes(monkeypatch, capsys):
+def test_command_line_modes(monkeypatch):
     import sys
 
     calls = {}
@@ -54,3 +54,30 @@ def test_command_line_modes(monkeypatch, capsys):
         assert list(calls) == [want]
         args = calls[want]
         assert args.warmup >= 3 and args.steps >= 1 and args.gpus == 1
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """The reference arm end to end on a small workload (10x5, K=64, 3 beams, whole
+    50-level searches): one JSON line with the contract's keys, labelled as the BS-PMS
+    semantics it runs, whose value is the oracle's scored children over the step time."""
+    import sys
+
+    from beamsearch_jssp_gpu_gb300.instance import synthetic_instance
+    from oracle import oracle as O
+
+    for k, v in (("N_JOBS", 10), ("N_MACH", 5), ("K", 64), ("BEAMS", 3), ("CPU_SAMPLE_LEVELS", 50)):
+        monkeypatch.setattr(bench, k, v)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1"])
+    assert bench.main() == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "candidates/s" and line["higher_is_better"]
+    assert line["metric"] == bench.METRIC and line["steps"] == 1 and line["warmup"] == 1
+    assert line["config"]["mode"] == "pms" and "cpu/v1_pms" in line["config"]["workload"]
+    assert line["e2e"] == {"value": line["value"], "unit": "candidates/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] == line["value"] and 1 <= cb["cores"] <= 3
+    mc, du = synthetic_instance(10, 5, bench.INSTANCE_SEED)
+    expanded = sum(O.solve(mc, du, "pms", 64, s)["expanded"] for s in range(3))
+    # one step: value = scored children of the 3 whole searches / the slowest beam's time
+    assert abs(line["value"] * line["ms_per_step"] / 1000.0 - expanded) <= 1e-6 * expanded

@@ -128,3 +128,29 @@ def test_rejections_at_submit():
         assert e.value.status == nat.BSJ_ERR_LIMIT
         t = srv.submit(mc, du, "v2", 64, 0)
         assert srv.wait(t)["found"]
+
+
+def test_prepared_plans_are_reused_by_later_requests(ctx):
+    """bsj_server_prepare builds plans of a shape before traffic; requests of that shape then
+    report built_plan = 0, a request of another shape builds its plan (built_plan = 1), and
+    every result still equals the plain solve."""
+    mc, du = synthetic_instance(20, 10, 5)
+    other = synthetic_instance(15, 5, 6)
+    with Server(0, max_inflight=4) as srv:
+        srv.prepare(mc, du, "v2", 256, copies=3)
+        deadline = time.time() + 60
+        while srv.stats()["plans_prepared"] < 3:
+            assert time.time() < deadline, "prepared plans not built within a minute"
+            time.sleep(0.01)
+        assert srv.stats()["plans_built"] == 3 and srv.stats()["completed"] == 0
+        tickets = [srv.submit(synthetic_instance(20, 10, 50 + k)[0], synthetic_instance(20, 10, 50 + k)[1], "v2",
+                              256, k) for k in range(3)]
+        got = [srv.wait(t) for t in tickets]
+        assert not any(g["built_plan"] for g in got)
+        for k, g in enumerate(got):
+            _same(g, ctx.solve(*synthetic_instance(20, 10, 50 + k), "v2", 256, k))
+        g = srv.wait(srv.submit(*other, "clean", 64, 9))
+        assert g["built_plan"]
+        _same(g, ctx.solve(*other, "clean", 64, 9))
+        st = srv.stats()
+        assert st["plans_built"] == 4 and st["plans_reused"] == 3 and st["completed"] == 4

@@ -64,7 +64,7 @@ def test_parser_matches_reference_parser(tmp_path):
 @needs_ref
 def test_reference_benchmark_files_parse_identically():
     """Lawrence / Taillard files are read by path only (never copied)."""
-    root = O.REF_TREE
+    root = O.reference_tree()
     paths = [os.path.join(root, "lawrence_instances", "la01.txt"),
              os.path.join(root, "taillard_instances", "ta01")]
     for p in paths:

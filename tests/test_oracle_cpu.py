@@ -161,3 +161,57 @@ def test_oracle_gpu_modes_match_reference_kernels(mode):
         assert k != "unexplained", r
         kinds[k] = kinds.get(k, 0) + 1
     assert kinds.get("equal", 0) > 0
+
+
+# ---- the benchmarked configuration: 50x20 / 100x20, K=4096, search seeds 0-7 ----------
+K4096 = os.path.join(os.path.dirname(__file__), "golden", "k4096.json")
+REF_GPU_K4096 = os.path.join(os.path.dirname(__file__), "golden", "ref_gpu_golden_k4096.json")
+
+
+def _k4096():
+    with open(K4096) as f:
+        cpu = json.load(f)
+    with open(REF_GPU_K4096) as f:
+        gpu = json.load(f)
+    return {(r["mode"], r["n"], r["seed"]): r for r in cpu["oracle"]}, cpu["reference_cpu"], gpu["records"]
+
+
+def test_k4096_oracle_records_equal_the_references():
+    """The committed oracle records at the benchmarked size equal every makespan of the
+    reference's own CPU solvers (BS-PMS 50x20 and 100x20, BS-ICH 50x20, 24 searches) and of
+    its gpu kernels run on a GB300 (v1 and v2, 50x20 and 100x20, 32 searches)."""
+    orc, ref_cpu, ref_gpu = _k4096()
+    assert len(ref_cpu) == 24 and len(ref_gpu) == 32
+    for r in ref_cpu:
+        assert orc[(r["mode"], r["n"], r["seed"])]["makespan"] == r["makespan"], r
+    for r in ref_gpu:
+        assert r["makespan_consistent"], r
+        assert orc[(r["mode"], r["n"], r["seed"])]["makespan"] == r["makespan"], r
+
+
+def _oracle_job(args):
+    mode, n, m, seed = args
+    mc, du = synthetic_instance(n, m, 0)
+    r = O.solve(mc, du, mode, 4096, seed)
+    import hashlib
+
+    return (int(r["makespan"]), int(r["expanded"]), int(r["slots"]), int(r["levels"]),
+            hashlib.sha256(np.ascontiguousarray(r["seq"], dtype="<i4").tobytes()).hexdigest())
+
+
+def test_k4096_oracle_reruns_match_its_records_and_the_reference():
+    """Three searches of the 50x20 benchmarked instance rerun here (BS-PMS seeds 0 and 1,
+    gpu-v2 seed 0), in parallel processes: each equals its committed record and the
+    reference's own result for it."""
+    import multiprocessing as mp
+
+    orc, ref_cpu, ref_gpu = _k4096()
+    jobs = [("pms", 50, 20, 0), ("pms", 50, 20, 1), ("v2", 50, 20, 0)]
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        out = pool.map(_oracle_job, jobs)
+    ref = {(r["mode"], r["n"], r["seed"]): r["makespan"] for r in ref_cpu + ref_gpu}
+    for (mode, n, m, seed), (mk, ex, sl, lv, sha) in zip(jobs, out):
+        rec = orc[(mode, n, seed)]
+        assert (mk, ex, sl, lv, sha) == (rec["makespan"], rec["expanded"], rec["slots"], rec["levels"],
+                                         rec["seq_sha256"])
+        assert mk == ref[(mode, n, seed)]
