@@ -588,6 +588,18 @@ struct TSnap {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// The snapshot layout and instance of one beam, in registers (the kernel writes global
+// memory inside its loops, so fields read through a SegDesc reference would be reloaded).
+struct TLay {
+    int n, m, N, sbytes, off_jr4, off_rd, off_nx, hw;
+    const uint32_t* ops;   // this instance's (duration << 8) | machine table
+    __device__ __forceinline__ TLay(const SegDesc& d, const uint32_t* all_ops)
+        : n(d.n), m(d.m), N(d.N), sbytes(d.sbytes), off_jr4(d.off_jr >> 2), off_rd(d.off_rd),
+          off_nx(d.off_nx), hw(d.off_hdr >> 2), ops(all_ops + d.op_off) {}
+    __device__ __forceinline__ uint32_t op(int j, int k) const { return __ldg(ops + j * m + k); }
+};
+
+// 16-byte loads of a snapshot into a lane's slot, four in flight at a time.
 template <int XS>
 __device__ __forceinline__ void tsnap_load(const TSnap<XS>& S, const uint8_t* src, int w16)
 {
@@ -614,6 +626,16 @@ __device__ __forceinline__ void tsnap_load(const TSnap<XS>& S, const uint8_t* sr
     }
 }
 
+// Asynchronous word copies of a snapshot into a lane's interleaved slot: every copy in
+// flight at once (one memory round trip); the caller commits and waits.
+__device__ __forceinline__ void tsnap_copy_async(uint32_t* w_il, const uint8_t* src, int words)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(w_il);
+    for (int x = 0; x < words; x++)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa + 128u * (unsigned)x), "l"(src + 4 * x)
+                     : "memory");
+}
+
 template <int XS>
 __device__ __forceinline__ void tsnap_store(const TSnap<XS>& S, uint8_t* dst, int w16)
 {
@@ -624,10 +646,10 @@ __device__ __forceinline__ void tsnap_store(const TSnap<XS>& S, uint8_t* dst, in
 
 // Job-predecessor finish (pred_finish above, on a lane's snapshot).
 template <int XS>
-__device__ __forceinline__ int tpred_finish(const TSnap<XS>& S, const SegDesc& d, int j, int k)
+__device__ __forceinline__ int tpred_finish(const TSnap<XS>& S, const TLay& L, int j, int k)
 {
-    if (d.m == 1) return j > 0 ? (int)S.word((d.off_jr >> 2) + j - 1) : 0;
-    return k == 0 ? 0 : (int)S.word((d.off_jr >> 2) + j);
+    if (L.m == 1) return j > 0 ? (int)S.word(L.off_jr4 + j - 1) : 0;
+    return k == 0 ? 0 : (int)S.word(L.off_jr4 + j);
 }
 
 // Ready position of the b-th candidate of the expansion of this (parent) snapshot at
@@ -635,18 +657,17 @@ __device__ __forceinline__ int tpred_finish(const TSnap<XS>& S, const SegDesc& d
 // parent has at most b candidates.  Only filler ranks need it (a scored child's position
 // comes from the table its parent's expansion wrote).
 template <int XS>
-__device__ int tnth_candidate(const TSnap<XS>& S, const SegDesc& d, const uint32_t* ops, uint32_t seed_t,
-                              int c, int b)
+__device__ int tnth_candidate(const TSnap<XS>& S, const TLay& L, uint32_t seed_t, int c, int b)
 {
-    const int rr = (int)(S.word(d.off_hdr >> 2) & 0xFFFFu);
+    const int rr = (int)(S.word(L.hw) & 0xFFFFu);
     if (rr <= 0) return -1;
     const uint32_t h = pivot_hash(seed_t + (uint32_t)c);
-    const int jp = S.byte(d.off_rd + (int)(h % (uint32_t)rr));
-    const int pm = (int)(__ldg(ops + d.op_off + jp * d.m + S.byte(d.off_nx + jp)) & 0xFFu);
+    const int jp = S.byte(L.off_rd + (int)(h % (uint32_t)rr));
+    const int pm = (int)(L.op(jp, S.byte(L.off_nx + jp)) & 0xFFu);
     int cnt = 0;
     for (int i = 0; i < rr; i++) {
-        const int j = S.byte(d.off_rd + i);
-        if ((int)(__ldg(ops + d.op_off + j * d.m + S.byte(d.off_nx + j)) & 0xFFu) == pm) {
+        const int j = S.byte(L.off_rd + i);
+        if ((int)(L.op(j, S.byte(L.off_nx + j)) & 0xFFu) == pm) {
             if (cnt == b) return i;
             cnt++;
         }
@@ -688,14 +709,23 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
             if (lane == 0) atomicOr(&st.status, kStatusBadSelect);
             continue;
         }
+        const TLay L(d, a.ops);
+        const int mode = d.mode, K = d.K, words = d.words, group = d.group;
+        const uint32_t seed = d.seed;
         const int q = chunk - __ldg(a.chunk_prefix + seg);
         const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
-        const int n = d.n, m = d.m, w16 = d.sbytes >> 4;
+        const int n = L.n, m = L.m, w16 = L.sbytes >> 4;
         const int r = q * 32 + lane;
         const bool act = r < P;
         uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
         const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
-        const int hw = d.off_hdr >> 2;
+        const uint8_t* pos_in = a.pos_pool + d.pos_off[s & 1];
+        uint8_t* pos_out = a.pos_pool + d.pos_off[(s + 1) & 1];
+        uint32_t* hist = a.hist + d.hist_off + (int64_t)(s < 0 ? 0 : s) * K;
+        uint32_t* masks = a.masks + d.mask_off;
+        unsigned long long* kdst0 = a.keys + d.key_off + (int64_t)q * 32 * n;
+        int32_t* kcnt = a.kcnt + d.kcnt_off + q;
+        const int bound = st.bound;
 
         // ---- 1. the source snapshot of this rank
         uint32_t e = 0;
@@ -713,15 +743,15 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
                 // the bulk copy's (async-proxy) write
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
-                             ::"r"(bar), "r"(d.sbytes) : "memory");
+                             ::"r"(bar), "r"(L.sbytes) : "memory");
                 asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                             ::"r"(smem_u32(S.w)), "l"(parent + (int64_t)c * d.sbytes), "r"(d.sbytes), "r"(bar)
+                             ::"r"(smem_u32(S.w)), "l"(parent + (int64_t)c * L.sbytes), "r"(L.sbytes), "r"(bar)
                              : "memory");
             } else {
                 asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar)
                              : "memory");
             }
-            if (act && s >= 0 && !(e & kFillerFlag)) ii = __ldg(a.pos_pool + d.pos_off[s & 1] + (e & ~kFillerFlag));
+            if (act && s >= 0 && !(e & kFillerFlag)) ii = __ldg(pos_in + (e & ~kFillerFlag));
             uint32_t done = 0;
             for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
                 asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -742,98 +772,105 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
             }
         } else {
             if (act && s >= 0) {
-                if (!(e & kFillerFlag)) ii = __ldg(a.pos_pool + d.pos_off[s & 1] + (e & ~kFillerFlag));
-                tsnap_load<XS>(S, parent + (int64_t)c * d.sbytes, w16);
+                tsnap_copy_async(S.w, parent + (int64_t)c * L.sbytes, L.sbytes >> 2);
+                if (!(e & kFillerFlag)) ii = __ldg(pos_in + (e & ~kFillerFlag));
             }
+            cp_async_commit();
+            cp_async_wait_all();
         }
 
         // ---- 2. materialise (v2: kernel_materialize_topk, gpu/v2_twophases/solver.cu:193-252)
         uint32_t hist_val = kMark;
         if (act && s < 0) {
-            for (int x = 0; x < (d.sbytes >> 2); x++) S.set_word(x, 0u);
-            for (int j = 0; j < n; j++) S.set_byte(d.off_rd + j, j);
-            S.set_word(hw, (uint32_t)n);
-            S.set_word(hw + 2, kMark);
+            for (int x = 0; x < (L.sbytes >> 2); x++) S.set_word(x, 0u);
+            for (int j = 0; j < n; j++) S.set_byte(L.off_rd + j, j);
+            S.set_word(L.hw, (uint32_t)n);
+            S.set_word(L.hw + 2, kMark);
             tsnap_store<XS>(S, childbuf, w16);
         } else if (act) {
-            if (e & kFillerFlag) ii = tnth_candidate<XS>(S, d, a.ops, d.seed + (uint32_t)s, c, b);
+            if (e & kFillerFlag) ii = tnth_candidate<XS>(S, L, seed + (uint32_t)s, c, b);
             if (ii >= 0) {
-                const uint32_t h0 = S.word(hw);
+                const uint32_t h0 = S.word(L.hw);
                 const int r0 = (int)(h0 & 0xFFFFu), ns = (int)(h0 >> 16);
-                const int j = S.byte(d.off_rd + ii);
-                const int k = S.byte(d.off_nx + j);
-                const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
+                const int j = S.byte(L.off_rd + ii);
+                const int k = S.byte(L.off_nx + j);
+                const uint32_t o = L.op(j, k);
                 const int mc = (int)(o & 0xFFu);
-                const int pred = tpred_finish<XS>(S, d, j, k);
+                const int pred = tpred_finish<XS>(S, L, j, k);
                 const int trv = (int)S.word(mc);
                 const int fin = (trv > pred ? trv : pred) + (int)(o >> 8);
-                const int lastj = S.byte(d.off_rd + r0 - 1);
+                const int lastj = S.byte(L.off_rd + r0 - 1);
                 const bool cont = (k + 1 < m);
-                const int cm = (int)S.word(hw + 1);
+                const int cm = (int)S.word(L.hw + 1);
                 S.set_word(mc, (uint32_t)fin);
-                S.set_word((d.off_jr >> 2) + j, (uint32_t)fin);
-                if (ii != r0 - 1) S.set_byte(d.off_rd + ii, lastj);
-                if (cont) S.set_byte(d.off_rd + r0 - 1, j);
-                S.set_byte(d.off_nx + j, k + 1);
-                S.set_word(hw, ((uint32_t)(ns + 1) << 16) | (uint32_t)(r0 - 1 + (cont ? 1 : 0)));
-                S.set_word(hw + 1, (uint32_t)(cm > fin ? cm : fin));
+                S.set_word(L.off_jr4 + j, (uint32_t)fin);
+                if (ii != r0 - 1) S.set_byte(L.off_rd + ii, lastj);
+                if (cont) S.set_byte(L.off_rd + r0 - 1, j);
+                S.set_byte(L.off_nx + j, k + 1);
+                S.set_word(L.hw, ((uint32_t)(ns + 1) << 16) | (uint32_t)(r0 - 1 + (cont ? 1 : 0)));
+                S.set_word(L.hw + 1, (uint32_t)(cm > fin ? cm : fin));
                 hist_val = ((uint32_t)c << 8) | (uint32_t)j;
-                S.set_word(hw + 2, hist_val);
-                S.set_word(hw + 3, (uint32_t)(s + 1));
-                tsnap_store<XS>(S, childbuf + (int64_t)r * d.sbytes, w16);
+                S.set_word(L.hw + 2, hist_val);
+                S.set_word(L.hw + 3, (uint32_t)(s + 1));
+                tsnap_store<XS>(S, childbuf + (int64_t)r * L.sbytes, w16);
             } else {
                 // filler rank whose branch does not exist: v2 leaves the ping-pong slot as
                 // it was (gpu/v2_twophases/solver.cu:191) and expands what it holds
-                if (d.mode == MODE_CLEAN) atomicOr(&st.status, kStatusBadSelect);
-                tsnap_load<XS>(S, childbuf + (int64_t)r * d.sbytes, w16);
+                if (mode == MODE_CLEAN) atomicOr(&st.status, kStatusBadSelect);
+                tsnap_load<XS>(S, childbuf + (int64_t)r * L.sbytes, w16);
             }
-            a.hist[d.hist_off + (int64_t)s * d.K + r] = hist_val;
+            hist[r] = hist_val;
         }
 
         // ---- 3. expand for level t (kernel_score_candidates, gpu/v2_twophases/solver.cu:68-123)
         const int t = s + 1;
-        const uint32_t seed_t = d.seed + (uint32_t)t;
-        const bool lastlv = (t == d.N - 1);
-        int cnt = 0, pm = -1, trp = 0, pcmax = 0, ns1 = 1;
+        const uint32_t seed_t = seed + (uint32_t)t;
+        const bool lastlv = (t == L.N - 1);
+        int cnt = 0, trp = 0, pcmax = 0, ns1 = 1;
         uint32_t vm0 = 0u, vm1 = 0u, vm2 = 0u, vm3 = 0u;
-        const int rr = act ? (int)(S.word(hw) & 0xFFFFu) : 0;
-        const int bound = st.bound;
+        const int rr = act ? (int)(S.word(L.hw) & 0xFFFFu) : 0;
         if (rr > 0) {
-            const uint32_t h0 = S.word(hw);
+            const uint32_t h0 = S.word(L.hw);
             ns1 = (int)(h0 >> 16) + 1;
-            pcmax = (int)S.word(hw + 1);
+            pcmax = (int)S.word(L.hw + 1);
             const uint32_t h = pivot_hash(seed_t + (uint32_t)r);
-            const int jp = S.byte(d.off_rd + (int)(h % (uint32_t)rr));
-            pm = (int)(__ldg(a.ops + d.op_off + jp * m + S.byte(d.off_nx + jp)) & 0xFFu);
+            const int jp = S.byte(L.off_rd + (int)(h % (uint32_t)rr));
+            const int pm = (int)(L.op(jp, S.byte(L.off_nx + jp)) & 0xFFu);
             trp = (int)S.word(pm);
-            uint8_t* prow = a.pos_pool + d.pos_off[t & 1] + (int64_t)r * n;
-            const bool rows = t < d.N - 1;
+            uint8_t* prow = pos_out + (int64_t)r * n;
+            const bool rows = t < L.N - 1;
             for (int i0 = 0; i0 < rr; i0 += 4) {
                 // off_rd = 4m + 4n is a multiple of 4: ready positions i0..i0+3 share a word
-                const uint32_t w4 = S.word((d.off_rd + i0) >> 2);
+                const uint32_t w4 = S.word((L.off_rd + i0) >> 2);
+                uint32_t ou[4];
+                int ju[4], ku[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    const int i = i0 + u;
-                    if (i < rr) {
-                        const int j = (int)((w4 >> (8 * u)) & 0xFFu);
-                        const int k = S.byte(d.off_nx + j);
-                        const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
-                        if ((int)(o & 0xFFu) == pm) {
-                            const int pred = tpred_finish<XS>(S, d, j, k);
-                            const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
-                            const int cmx = pcmax > fin ? pcmax : fin;
-                            if (cmx < bound) {   // gpu/v1/solver.cu:120
-                                const uint32_t bit = 1u << (cnt & 31);
-                                const int wq = cnt >> 5;
-                                vm0 |= (wq == 0) ? bit : 0u;
-                                vm1 |= (wq == 1) ? bit : 0u;
-                                vm2 |= (wq == 2) ? bit : 0u;
-                                vm3 |= (wq == 3) ? bit : 0u;
-                            }
-                            posl[cnt * 32] = (uint8_t)i;
-                            if (rows) prow[cnt] = (uint8_t)i;
-                            cnt++;
+                    ju[u] = (int)((w4 >> (8 * u)) & 0xFFu);
+                    ku[u] = 0;
+                    ou[u] = 0xFFu;
+                    if (i0 + u < rr) {
+                        ku[u] = S.byte(L.off_nx + ju[u]);
+                        ou[u] = L.op(ju[u], ku[u]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (i0 + u < rr && (int)(ou[u] & 0xFFu) == pm) {
+                        const int pred = tpred_finish<XS>(S, L, ju[u], ku[u]);
+                        const int fin = (trp > pred ? trp : pred) + (int)(ou[u] >> 8);
+                        const int cmx = pcmax > fin ? pcmax : fin;
+                        if (cmx < bound) {   // gpu/v1/solver.cu:120
+                            const uint32_t bit = 1u << (cnt & 31);
+                            const int wq = cnt >> 5;
+                            vm0 |= (wq == 0) ? bit : 0u;
+                            vm1 |= (wq == 1) ? bit : 0u;
+                            vm2 |= (wq == 2) ? bit : 0u;
+                            vm3 |= (wq == 3) ? bit : 0u;
                         }
+                        posl[cnt * 32] = (uint8_t)(i0 + u);
+                        if (rows) prow[cnt] = (uint8_t)(i0 + u);
+                        cnt++;
                     }
                 }
             }
@@ -851,21 +888,20 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
         if (act) {
 #pragma unroll
             for (int w = 0; w < 4; w++)
-                if (w < d.words)
-                    a.masks[d.mask_off + (int64_t)r * d.words + w] = w == 0 ? vm0 : (w == 1 ? vm1 : (w == 2 ? vm2 : vm3));
+                if (w < words) masks[(int64_t)r * words + w] = w == 0 ? vm0 : (w == 1 ? vm1 : (w == 2 ? vm2 : vm3));
         }
         if (nv > 0) {
-            unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * 32 * n + pre;
+            unsigned long long* kdst = kdst0 + pre;
             const float fns = __int2float_rn(ns1);
             int o_k = 0;
             for (int bb = 0; bb < cnt; bb++) {
                 const uint32_t vw = (bb >> 5) == 0 ? vm0 : ((bb >> 5) == 1 ? vm1 : ((bb >> 5) == 2 ? vm2 : vm3));
                 if (!((vw >> (bb & 31)) & 1u)) continue;
                 const int i = posl[bb * 32];
-                const int j = S.byte(d.off_rd + i);
-                const int k = S.byte(d.off_nx + j);
-                const uint32_t o = __ldg(a.ops + d.op_off + j * m + k);
-                const int pred = tpred_finish<XS>(S, d, j, k);
+                const int j = S.byte(L.off_rd + i);
+                const int k = S.byte(L.off_nx + j);
+                const uint32_t o = L.op(j, k);
+                const int pred = tpred_finish<XS>(S, L, j, k);
                 const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
                 const int cmx = pcmax > fin ? pcmax : fin;
                 const float base = __fdiv_rn(__int2float_rn(cmx), fns);
@@ -873,14 +909,14 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
                 const float sc = __fadd_rn(base, __ldg(a.noise + ni));
                 const uint32_t slot = (uint32_t)(r * n + bb);
                 kdst[o_k++] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
-                if (lastlv && ns1 == d.N) {
+                if (lastlv && ns1 == L.N) {
                     atomicMin(&st.best, ((unsigned long long)(uint32_t)cmx << 32) |
                                             ((unsigned long long)slot << 8) | (uint32_t)j);
-                    atomicMin(a.group_best + d.group, cmx);
+                    atomicMin(a.group_best + group, cmx);
                 }
             }
         }
-        if (lane == 0) a.kcnt[d.kcnt_off + q] = total;
+        if (lane == 0) *kcnt = total;
         __syncwarp();
     }
 }
