@@ -526,7 +526,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             for (int v = 0; v < kNumStepVariants; v++) {
                 const int ci = chunk_var_of(kStepVariantChunk[v]);
                 int g = p->cprefix[ci][hi] - p->cprefix[ci][lo];
-                if (kStepVariantThread[v] && gr.thread_ok) g = (g + kTStepWarpsPerCta - 1) / kTStepWarpsPerCta;
+                const int tv = kStepVariantThread[v];
+                if ((tv == 1 || tv == 2) && gr.thread_ok) g = (g + kTStepWarpsPerCta - 1) / kTStepWarpsPerCta;
                 gr.step_grid[v] = std::max(1, std::min(g, 65535));
             }
             const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
@@ -1025,7 +1026,8 @@ bsj_status bsj_plan_set_chunk(bsj_plan* p, int32_t chunk)
         }
     }
     return fail(p->ctx, BSJ_ERR_INVALID,
-                "chunk must be 0 (default rule), 8, 16, 32 (warp per survivor) or 1, 2 (thread per survivor)");
+                "chunk must be 0 (default rule), 8, 16, 32 (warp per survivor), 1, 2 (thread per survivor) "
+                "or 3, 4, 5, 6 (lane group per survivor)");
 }
 
 static_assert(BSJ_SELECT_FORCE_LARGE == kSelForceLarge && BSJ_SELECT_NO_LARGE == kSelNoLarge &&

@@ -922,6 +922,305 @@ __global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
 }
 
 // ------------------------------------------------------------------------------------
+// k_step_g: materialise + expand with a GROUP of G lanes per survivor (gpu-v2 / clean
+// beams), 32/G survivors per warp, 4 warps per CTA: CH = 128/G consecutive ranks per CTA
+// (one key chunk of CH).  Between the warp form (every lane on one survivor: most lanes
+// idle) and the thread form (one lane per survivor: a long serial chain per lane), the
+// group splits what is long -- staging the parent, storing the child, scanning the ready
+// list -- and keeps what is short on the group's first lane (applying the selected op).
+// Candidates are numbered in ready-list order with group-masked ballots, scored by the
+// lane that found them and staged per survivor in shared memory; the CTA copies its
+// chunk's keys out in slot order.
+// Staging of the parent snapshot (template STG): 1 = 16-byte cp.async by the group's lanes;
+// 2 = one cp.async.bulk (TMA bulk copy) per survivor issued by the group's first lane,
+// completing on a per-warp mbarrier.
+// Result-identical to k_step (same arithmetic in the same order per child).
+// ------------------------------------------------------------------------------------
+constexpr int kGStepWarps = 4;
+
+__host__ __device__ __forceinline__ size_t gstep_smem_bytes(int G, int sb_max, int max_n)
+{
+    const size_t ch = (size_t)kGStepWarps * (size_t)(32 / G);
+    return ch * (size_t)sb_max + ch * (size_t)max_n * 8;
+}
+
+template <int G, int STG>
+__global__ void __launch_bounds__(kGStepWarps * 32) k_step_g(StepArgs a, int s)
+{
+    constexpr int SPW = 32 / G;            // survivors per warp
+    constexpr int CH = kGStepWarps * SPW;  // survivors per CTA = key chunk size
+    constexpr bool BULK = (STG == 2);
+    constexpr unsigned kLowG = (1u << G) - 1u;
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ __align__(8) unsigned long long s_mbar[kGStepWarps];
+    __shared__ int s_nv[CH], s_pre[CH], s_kcnt, s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / G, gl = lane % G, gsh = grp * G;
+    const int slot = warp * SPW + grp;
+    const unsigned ltg = (1u << gl) - 1u;
+    uint8_t* sb = smem + (size_t)slot * a.sb_max;
+    unsigned long long* kst =
+        reinterpret_cast<unsigned long long*>(smem + (size_t)CH * a.sb_max) + (size_t)slot * a.max_n;
+    TSnap<1> S;
+    S.w = reinterpret_cast<uint32_t*>(sb);
+    pdl_trigger();
+    if (BULK) {
+        if (lane == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&s_mbar[warp])), "r"(32) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncwarp();
+    }
+    if (threadIdx.x == 0) s_abort = 0;
+    __syncthreads();
+    uint32_t phase = 0;
+    pdl_wait();
+    for (int chunk = a.chunk_lo + blockIdx.x; chunk < a.chunk_hi; chunk += gridDim.x) {
+        const int seg = find_seg(a.chunk_prefix, a.seg_lo, a.seg_hi, chunk);
+        const SegDesc& d = a.segs[seg];
+        if (s >= d.N - 1) continue;   // the same for the whole CTA (one chunk)
+        SegState& st = a.st[seg];
+        if (d.mode != MODE_V2 && d.mode != MODE_CLEAN) {   // the host runs only these beams here
+            if (threadIdx.x == 0) atomicOr(&st.status, kStatusBadSelect);
+            continue;
+        }
+        const TLay L(d, a.ops);
+        const int mode = d.mode, K = d.K, words = d.words, group = d.group;
+        const uint32_t seed = d.seed;
+        const int q = chunk - __ldg(a.chunk_prefix + seg);
+        const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
+        const int n = L.n, m = L.m, w16 = L.sbytes >> 4;
+        const int r = q * CH + slot;
+        const bool act = r < P;
+        uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
+        const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
+        const uint8_t* pos_in = a.pos_pool + d.pos_off[s & 1];
+        uint8_t* pos_out = a.pos_pool + d.pos_off[(s + 1) & 1];
+        const int bound = st.bound;
+
+        // ---- 1. the source snapshot of this rank
+        uint32_t e = 0;
+        int c = 0, b = 0, ii = -1;
+        if (act && s >= 0) {
+            e = __ldg(a.sel + d.sel_off + r);
+            const uint32_t sl = e & ~kFillerFlag;
+            c = (int)(sl / (uint32_t)n);
+            b = (int)sl - c * n;
+            if (!(e & kFillerFlag)) ii = __ldg(pos_in + sl);
+        }
+        const uint8_t* src = parent + (int64_t)c * L.sbytes;
+        bool ok = true;
+        if (BULK) {
+            const uint32_t bar = smem_u32(&s_mbar[warp]);
+            if (gl == 0 && act && s >= 0) {
+                // the slot was last written through the generic proxy: order that before
+                // the bulk copy's (async-proxy) write
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
+                             ::"r"(bar), "r"(L.sbytes) : "memory");
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                             ::"r"(smem_u32(sb)), "l"(src), "r"(L.sbytes), "r"(bar) : "memory");
+            } else {
+                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar)
+                             : "memory");
+            }
+            uint32_t done = 0;
+            for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
+                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                             " selp.u32 %0, 1, 0, p;\n}\n"
+                             : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+            }
+            phase ^= 1u;
+            if (!__all_sync(FULL_MASK, done)) {
+                // a copy that never completed: flag it, wait once more (bounded) for the
+                // warp's copies, take no part in this chunk and make the CTA stop after it
+                // (every warp still reaches the chunk's barriers)
+                if (lane == 0) {
+                    atomicOr(&st.status, kStatusBadSelect);
+                    s_abort = 1;
+                }
+                for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
+                    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                                 " selp.u32 %0, 1, 0, p;\n}\n"
+                                 : "=r"(done) : "r"(bar), "r"(phase ^ 1u) : "memory");
+                }
+                ok = false;
+            }
+        } else {
+            if (act && s >= 0)
+                for (int x = gl; x < w16; x += G) cp_async16(sb + 16 * x, src + 16 * x);
+            cp_async_commit();
+            cp_async_wait_all();
+        }
+        __syncwarp();
+        const bool live = act && ok;
+
+        // ---- 2. materialise (v2: kernel_materialize_topk, gpu/v2_twophases/solver.cu:193-252)
+        // a filler's branch position comes from the parent's expansion, recomputed
+        int fii = -1;
+        if (gl == 0 && live && s >= 0 && (e & kFillerFlag))
+            fii = tnth_candidate<1>(S, L, seed + (uint32_t)s, c, b);
+        fii = __shfl_sync(FULL_MASK, fii, gsh);
+        if (e & kFillerFlag) ii = fii;
+        const bool do_root = live && s < 0;
+        const bool do_apply = live && s >= 0 && ii >= 0;
+        const bool do_stale = live && s >= 0 && ii < 0;
+        uint32_t hist_val = kMark;
+        if (gl == 0 && do_root) {
+            for (int x = 0; x < (L.sbytes >> 2); x++) S.set_word(x, 0u);
+            for (int j = 0; j < n; j++) S.set_byte(L.off_rd + j, j);
+            S.set_word(L.hw, (uint32_t)n);
+            S.set_word(L.hw + 2, kMark);
+        }
+        if (gl == 0 && do_apply) {
+            const uint32_t h0 = S.word(L.hw);
+            const int r0 = (int)(h0 & 0xFFFFu), ns = (int)(h0 >> 16);
+            const int j = S.byte(L.off_rd + ii);
+            const int k = S.byte(L.off_nx + j);
+            const uint32_t o = L.op(j, k);
+            const int mc = (int)(o & 0xFFu);
+            const int pred = tpred_finish<1>(S, L, j, k);
+            const int trv = (int)S.word(mc);
+            const int fin = (trv > pred ? trv : pred) + (int)(o >> 8);
+            const int lastj = S.byte(L.off_rd + r0 - 1);
+            const bool cont = (k + 1 < m);
+            const int cm = (int)S.word(L.hw + 1);
+            S.set_word(mc, (uint32_t)fin);
+            S.set_word(L.off_jr4 + j, (uint32_t)fin);
+            if (ii != r0 - 1) S.set_byte(L.off_rd + ii, lastj);
+            if (cont) S.set_byte(L.off_rd + r0 - 1, j);
+            S.set_byte(L.off_nx + j, k + 1);
+            S.set_word(L.hw, ((uint32_t)(ns + 1) << 16) | (uint32_t)(r0 - 1 + (cont ? 1 : 0)));
+            S.set_word(L.hw + 1, (uint32_t)(cm > fin ? cm : fin));
+            hist_val = ((uint32_t)c << 8) | (uint32_t)j;
+            S.set_word(L.hw + 2, hist_val);
+            S.set_word(L.hw + 3, (uint32_t)(s + 1));
+        }
+        if (do_stale) {
+            // filler rank whose branch does not exist: v2 leaves the ping-pong slot as it
+            // was (gpu/v2_twophases/solver.cu:191) and expands what it holds
+            const uint4* s4 = reinterpret_cast<const uint4*>(childbuf + (int64_t)r * L.sbytes);
+            for (int x = gl; x < w16; x += G) reinterpret_cast<uint4*>(sb)[x] = __ldcg(s4 + x);
+            if (gl == 0 && mode == MODE_CLEAN) atomicOr(&st.status, kStatusBadSelect);
+        }
+        __syncwarp();
+        if (do_root || do_apply) {
+            uint4* d4 = reinterpret_cast<uint4*>(childbuf + (int64_t)r * L.sbytes);
+            for (int x = gl; x < w16; x += G) d4[x] = reinterpret_cast<const uint4*>(sb)[x];
+        }
+        if (gl == 0 && live && s >= 0) a.hist[d.hist_off + (int64_t)s * K + r] = hist_val;
+
+        // ---- 3. expand for level t (kernel_score_candidates, gpu/v2_twophases/solver.cu:68-123)
+        const int t = s + 1;
+        const uint32_t seed_t = seed + (uint32_t)t;
+        const bool lastlv = (t == L.N - 1);
+        const bool rows = t < L.N - 1;
+        const int rr = live ? (int)(S.word(L.hw) & 0xFFFFu) : 0;
+        const int rrmax = __reduce_max_sync(FULL_MASK, (unsigned)rr);
+        int ns1 = 1, pcmax = 0, trp = 0, pm = -1;
+        if (rr > 0) {
+            const uint32_t h0 = S.word(L.hw);
+            ns1 = (int)(h0 >> 16) + 1;
+            pcmax = (int)S.word(L.hw + 1);
+            const uint32_t h = pivot_hash(seed_t + (uint32_t)r);
+            const int jp = S.byte(L.off_rd + (int)(h % (uint32_t)rr));
+            pm = (int)(L.op(jp, S.byte(L.off_nx + jp)) & 0xFFu);
+            trp = (int)S.word(pm);
+        }
+        const float fns = __int2float_rn(ns1);
+        uint8_t* prow = pos_out + (int64_t)r * n;
+        int carry = 0, vcarry = 0;
+        uint32_t vm0 = 0u, vm1 = 0u, vm2 = 0u, vm3 = 0u;
+        for (int i0 = 0; i0 < rrmax; i0 += G) {
+            const int i = i0 + gl;
+            bool on = false, valid = false;
+            int j = 0, cmx = 0;
+            if (i < rr) {
+                j = S.byte(L.off_rd + i);
+                const int k = S.byte(L.off_nx + j);
+                const uint32_t o = L.op(j, k);
+                on = (int)(o & 0xFFu) == pm;
+                if (on) {
+                    const int pred = tpred_finish<1>(S, L, j, k);
+                    const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
+                    cmx = pcmax > fin ? pcmax : fin;
+                    valid = cmx < bound;   // gpu/v1/solver.cu:120
+                }
+            }
+            const unsigned gb = (__ballot_sync(FULL_MASK, on) >> gsh) & kLowG;
+            const unsigned gv = (__ballot_sync(FULL_MASK, valid) >> gsh) & kLowG;
+            if (on) {
+                const int bidx = carry + __popc(gb & ltg);
+                if (rows) prow[bidx] = (uint8_t)i;
+                if (valid) {
+                    const int vidx = vcarry + __popc(gv & ltg);
+                    const float base = __fdiv_rn(__int2float_rn(cmx), fns);
+                    const uint32_t ni = noise_hash(seed_t, (uint32_t)r, (uint32_t)bidx) % 1000u;
+                    const float sc = __fadd_rn(base, __ldg(a.noise + ni));
+                    const uint32_t sl = (uint32_t)(r * n + bidx);
+                    kst[vidx] = ((unsigned long long)__float_as_uint(sc) << 32) | sl;
+                    const uint32_t bit = 1u << (bidx & 31);
+                    const int wq = bidx >> 5;
+                    vm0 |= (wq == 0) ? bit : 0u;
+                    vm1 |= (wq == 1) ? bit : 0u;
+                    vm2 |= (wq == 2) ? bit : 0u;
+                    vm3 |= (wq == 3) ? bit : 0u;
+                    if (lastlv && ns1 == L.N) {
+                        atomicMin(&st.best, ((unsigned long long)(uint32_t)cmx << 32) |
+                                                ((unsigned long long)sl << 8) | (uint32_t)j);
+                        atomicMin(a.group_best + group, cmx);
+                    }
+                }
+            }
+            carry += __popc(gb);
+            vcarry += __popc(gv);
+        }
+        // the group's scored-branch mask words (lanes of a group differ in their low bits)
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            vm0 |= __shfl_xor_sync(FULL_MASK, vm0, o);
+            vm1 |= __shfl_xor_sync(FULL_MASK, vm1, o);
+            vm2 |= __shfl_xor_sync(FULL_MASK, vm2, o);
+            vm3 |= __shfl_xor_sync(FULL_MASK, vm3, o);
+        }
+        if (gl == 0) {
+            s_nv[slot] = live ? vcarry : 0;
+            if (live) {
+#pragma unroll
+                for (int w = 0; w < 4; w++)
+                    if (w < words)
+                        a.masks[d.mask_off + (int64_t)r * words + w] =
+                            w == 0 ? vm0 : (w == 1 ? vm1 : (w == 2 ? vm2 : vm3));
+            }
+        }
+        __syncthreads();
+        // ---- 4. the chunk's keys out in slot order
+        if (warp == 0) {
+            const int v = lane < CH ? s_nv[lane] : 0;
+            int x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane < CH) s_pre[lane] = x - v;
+            if (lane == 31) s_kcnt = x;
+        }
+        __syncthreads();
+        unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * CH * n;
+        for (int rl = warp; rl < CH; rl += kGStepWarps) {
+            const int cntk = s_nv[rl], dst0 = s_pre[rl];
+            const unsigned long long* ks =
+                reinterpret_cast<const unsigned long long*>(smem + (size_t)CH * a.sb_max) + (size_t)rl * a.max_n;
+            for (int x = lane; x < cntk; x += 32) kdst[dst0 + x] = ks[x];
+        }
+        if (threadIdx.x == 0) a.kcnt[d.kcnt_off + q] = s_kcnt;
+        __syncthreads();
+        if (s_abort) break;
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // k_select: exact top-K + stable order per beam (gpu modes).
 //
 // The reference sorts all P*n (score, slot) pairs with a stable radix sort and keeps the
@@ -2221,16 +2520,19 @@ int heap_pick_chunk(HeapCfg c, size_t budget)
     return 0;
 }
 
-// libstdc++ __push_heap: the value rises from `hole` while its parent is smaller.
+// libstdc++ __push_heap: the value rises from `hole` while its parent is smaller.  The
+// parent's value is loaded with its key, so a move costs one shared-memory round trip.
 __device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* hv, int hole, int top,
                                              unsigned long long vk, uint32_t vv)
 {
-    int parent = (hole - 1) / 2;
-    while (hole > top && hk[parent] < vk) {
-        hk[hole] = hk[parent];
-        hv[hole] = hv[parent];
+    while (hole > top) {
+        const int parent = (hole - 1) / 2;
+        const unsigned long long kp = hk[parent];
+        const uint32_t vp = hv[parent];
+        if (!(kp < vk)) break;
+        hk[hole] = kp;
+        hv[hole] = vp;
         hole = parent;
-        parent = (hole - 1) / 2;
     }
     hk[hole] = vk;
     hv[hole] = vv;
@@ -2238,6 +2540,10 @@ __device__ __forceinline__ void heap_sift_up(unsigned long long* hk, uint32_t* h
 
 // libstdc++ __adjust_heap: the hole walks down to a leaf along the larger children (the
 // right one on ties, a lone left child is taken), then the value is pushed up from there.
+// Both children's keys and values are loaded together, so each level of the walk costs
+// one shared-memory round trip (the value no longer waits for the comparison).  (Loading
+// the four grandchildren as well, two levels per round, measured slower: 4.94 vs 4.64 s
+// per 8-beam BS-PMS search at 50x20, K=4096 -- the heap thread is issue-bound by then.)
 __device__ void heap_adjust(unsigned long long* hk, uint32_t* hv, int hole, int len,
                             unsigned long long vk, uint32_t vv)
 {
@@ -2245,9 +2551,12 @@ __device__ void heap_adjust(unsigned long long* hk, uint32_t* hv, int hole, int 
     int child = hole;
     while (child < (len - 1) / 2) {
         child = 2 * (child + 1);
-        if (hk[child] < hk[child - 1]) child--;
-        hk[hole] = hk[child];
-        hv[hole] = hv[child];
+        const unsigned long long kr = hk[child], kl = hk[child - 1];
+        const uint32_t vr = hv[child], vl = hv[child - 1];
+        const bool left = kr < kl;
+        child -= left ? 1 : 0;
+        hk[hole] = left ? kl : kr;
+        hv[hole] = left ? vl : vr;
         hole = child;
     }
     if ((len & 1) == 0 && child == (len - 2) / 2) {
@@ -2712,6 +3021,16 @@ static cudaError_t for_each_tstep(F&& f)
     return e;
 }
 
+template <typename F>
+static cudaError_t for_each_gstep(F&& f)
+{
+    cudaError_t e = f(k_step_g<4, 1>, 4);
+    if (e == cudaSuccess) e = f(k_step_g<4, 2>, 4);
+    if (e == cudaSuccess) e = f(k_step_g<8, 1>, 8);
+    if (e == cudaSuccess) e = f(k_step_g<8, 2>, 8);
+    return e;
+}
+
 int nq_class(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
 
 // All level kernels run back to back; giving them one shared-memory carveout (the
@@ -2725,6 +3044,8 @@ static cudaError_t set_carveout()
         e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess)
         e = for_each_tstep([&](auto fn) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
+    if (e == cudaSuccess)
+        e = for_each_gstep([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gather_v1, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     return e;
@@ -2754,6 +3075,8 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
+    if (e == cudaSuccess)
+        e = for_each_gstep([&](auto fn, int g) { return raise_smem(fn, gstep_smem_bytes(g, sb_max, max_n)); });
     return e;
 }
 
@@ -2764,6 +3087,8 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
+    if (e == cudaSuccess)
+        e = for_each_gstep([&](auto fn, int g) { return raise_smem(fn, gstep_smem_bytes(g, sb_max, max_n)); });
     return e;
 }
 
@@ -2806,6 +3131,19 @@ static cudaError_t launch_step_ch(const StepArgs& a, int s, int grid, int nq_mas
 
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
+    if (a.thread_step >= 3) {
+        const int G = a.thread_step <= 4 ? 4 : 8;
+        if (a.chunk != kGStepWarps * (32 / G)) return cudaErrorInvalidValue;
+        const size_t sm = gstep_smem_bytes(G, a.sb_max, a.max_n);
+        const int block = kGStepWarps * 32;
+        switch (a.thread_step) {
+        case 3: return launch_kernel(k_step_g<4, 1>, grid, block, sm, stream, s >= 0, a, s);
+        case 4: return launch_kernel(k_step_g<4, 2>, grid, block, sm, stream, s >= 0, a, s);
+        case 5: return launch_kernel(k_step_g<8, 1>, grid, block, sm, stream, s >= 0, a, s);
+        case 6: return launch_kernel(k_step_g<8, 2>, grid, block, sm, stream, s >= 0, a, s);
+        default: return cudaErrorInvalidValue;
+        }
+    }
     if (a.thread_step) {
         if (a.chunk != 32) return cudaErrorInvalidValue;
         const size_t sm = tstep_smem_bytes(a.sb_max, a.max_n);

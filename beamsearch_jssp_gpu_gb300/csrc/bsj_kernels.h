@@ -46,13 +46,15 @@ struct StepArgs {
 
 // k_step variants (the autotuner's candidates besides the default rule): warp per
 // survivor with 8, 16 or 32 survivors per CTA; one thread per survivor (32 per warp, key
-// chunks of 32) with the parent snapshots staged by 16-byte loads or by bulk copies.
-// Thread variants apply to beam groups whose beams are all gpu-v2 / clean; other groups
-// run the warp kernel with 32 per CTA.  Public codes (bsj_plan_set_chunk): 8, 16, 32, 1, 2.
-constexpr int kNumStepVariants = 5;
-constexpr int kStepVariantChunk[kNumStepVariants] = {8, 16, 32, 32, 32};
-constexpr int kStepVariantThread[kNumStepVariants] = {0, 0, 0, 1, 2};
-constexpr int kStepVariantCode[kNumStepVariants] = {8, 16, 32, 1, 2};
+// chunks of 32) with the parent snapshots staged by word copies or by bulk copies; a group
+// of 4 lanes per survivor (32 per CTA) or of 8 lanes (16 per CTA), parents staged by the
+// group's 16-byte copies or by one bulk copy.  Thread and group variants apply to beam
+// groups whose beams are all gpu-v2 / clean; other groups run the warp kernel with the
+// same chunk size.  Public codes (bsj_plan_set_chunk): 8, 16, 32, 1, 2, 3, 4, 5, 6.
+constexpr int kNumStepVariants = 9;
+constexpr int kStepVariantChunk[kNumStepVariants] = {8, 16, 32, 32, 32, 32, 32, 16, 16};
+constexpr int kStepVariantThread[kNumStepVariants] = {0, 0, 0, 1, 2, 3, 4, 5, 6};
+constexpr int kStepVariantCode[kNumStepVariants] = {8, 16, 32, 1, 2, 3, 4, 5, 6};
 constexpr int kTStepWarpsPerCta = 4;   // k_step_t: warps (32-survivor chunks) per CTA
 
 // k_heap launch configuration: the largest K, child-table row (bytes) and n of the

@@ -33,8 +33,11 @@ Also on the JSON line (rank 0; --no-extras skips them):
              batch's k_step chunk sizes are autotuned on its first call (untimed);
   "serving"  400 requests with Poisson arrivals through bsj_server (continuous
              batching) at 150/s (sustained) and 1000/s (overload), solves/s and p50/p99
-             latency per rate against the plain path on the same requests, results
-             compared.
+             latency per rate (also split by requests that reused / built a plan) against
+             the plain path on the same requests, results compared; plans of every shape
+             are prepared before the timed streams;
+  "serving_mixed_branching"  96 requests, half BS-ICH / BS-PMS (K=256), half gpu-v2 /
+             clean, at 40/s: solves/s, p50/p99 overall and per mode, results compared.
 
 Multi-GPU: replicas only (each rank runs its own 8 beams; no collective on the data
 path); value = all ranks' candidates / max-over-ranks time.
@@ -273,8 +276,12 @@ def gpu_arm(args) -> int:
 
     with torch.cuda.stream(stream):
         plan.set_timing(False)
-        # autotuner: k_step chunk size for this shape (untimed; results do not depend on it)
-        tune = plan.autotune(repeats=1, stream=sh)
+        if args.step_form is None:
+            # autotuner: k_step form for this shape (untimed; results do not depend on it)
+            tune = plan.autotune(repeats=1, stream=sh)
+        else:
+            plan.chunk = args.step_form
+            tune = {"chunk": args.step_form, "ms": {}}
         for _ in range(args.warmup):
             plan.run(sh)
         torch.cuda.synchronize()
@@ -350,6 +357,7 @@ def gpu_arm(args) -> int:
         extras["pms_exact"] = pms_exact(ctx, mc, du, stream)
         extras["batched"] = batched_stream(ctx)
         extras["serving"] = served_stream(ctx, local)
+        extras["serving_mixed_branching"] = served_mixed_branching(ctx, local)
 
     if rank == 0 and cpu:
         extras["cpu_baseline_pms"] = cpu_pms
@@ -441,11 +449,78 @@ def batched_stream(ctx, count: int = 256, seed: int = 1) -> dict:
             "expanded_per_s": sum(r["expanded"] for r in out) / t_batch}
 
 
+def _serve(srv, reqs, rate: float, seed: int):
+    """Open-loop Poisson arrivals of `reqs` at `rate`; returns the results in request order
+    and the span from the first submission to the last result."""
+    import numpy as np
+
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, len(reqs))
+    tickets = []
+    t0 = time.perf_counter()
+    arrival = t0
+    for r, g in zip(reqs, gaps):
+        arrival += g
+        while time.perf_counter() < arrival:
+            pass
+        tickets.append(srv.submit(*r))
+    got = [srv.wait(t) for t in tickets]
+    return got, time.perf_counter() - t0
+
+
+def _plain(ctx, reqs):
+    """The plain path: every request solved alone, one call at a time (bsj_solve); returns
+    the results, each request's own solve time (ms) and the total seconds."""
+    out, ms = [], []
+    t0 = time.perf_counter()
+    for r in reqs:
+        t1 = time.perf_counter()
+        out.append(ctx.solve(*r))
+        ms.append(1000.0 * (time.perf_counter() - t1))
+    return out, ms, time.perf_counter() - t0
+
+
+def _latency(got, solo_ms=None) -> dict:
+    """p50/p99 of queue + run time, over all requests and split by whether the request found
+    an idle plan of its shape or built one; with `solo_ms` (each request's time solved alone)
+    also the stretch, latency / solo time, which removes the spread of search lengths in the
+    mix (a 100x20 K=4096 search takes ~30x a 15x15 K=256 one)."""
+    import numpy as np
+
+    out = {}
+    if solo_ms is not None:
+        st = np.array([(g["queue_ms"] + g["run_ms"]) / max(1e-3, t) for g, t in zip(got, solo_ms)])
+        out["stretch"] = {"p50": float(np.percentile(st, 50)), "p99": float(np.percentile(st, 99))}
+    for name, sel in (("all", lambda g: True), ("reused_plan", lambda g: not g["built_plan"]),
+                      ("built_plan", lambda g: g["built_plan"])):
+        lat = np.array([g["queue_ms"] + g["run_ms"] for g in got if sel(g)])
+        out[name] = ({"count": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
+                      "p99_ms": float(np.percentile(lat, 99))} if lat.size else {"count": 0})
+    return out
+
+
+def _warm(srv, reqs, copies: int):
+    """Before traffic: `copies` prepared plans of every request shape (bsj_server_prepare),
+    as a long-running server holds for the shapes it serves."""
+    shapes = {}
+    for r in reqs:
+        shapes.setdefault((r[0].shape, r[2], r[3]), r)
+    for r in shapes.values():
+        srv.prepare(r[0], r[1], r[2], r[3], copies=copies, seed=r[4])
+    deadline = time.time() + 600
+    while srv.stats()["plans_prepared"] < copies * len(shapes):
+        if time.time() > deadline:
+            raise RuntimeError("prepared plans not ready within 10 minutes")
+        time.sleep(0.01)
+    return len(shapes)
+
+
 def served_stream(ctx, device: int, count: int = 400, rates=(150.0, 1000.0), inflight: int = 96,
-                  seed: int = 5) -> dict:
+                  seed: int = 5, warm_copies: int = 8) -> dict:
     """Open-loop Poisson arrivals served by bsj_server (continuous batching), at a rate the
     server sustains and at one it cannot (queueing), against the plain path solving the same
-    requests one at a time.  Every result is compared with the plain path's."""
+    requests one at a time.  Every result is compared with the plain path's.  Before the
+    timed streams the server prepares `warm_copies` plans of every request shape; latency is
+    reported over all requests and split by requests that reused a plan / built one."""
     import random
 
     import numpy as np
@@ -461,45 +536,76 @@ def served_stream(ctx, device: int, count: int = 400, rates=(150.0, 1000.0), inf
         mode = rng.choice(["v2", "clean"])
         mc, du = synthetic_instance(n, m, 20000 + i)
         reqs.append((mc, du, mode, K, rng.randrange(1 << 30)))
-    t0 = time.perf_counter()
-    plain = [ctx.solve(*r) for r in reqs]
-    t_plain = time.perf_counter() - t0
+    plain, solo_ms, t_plain = _plain(ctx, reqs)
     runs = []
     same = True
     with Server(device, max_inflight=inflight) as srv:
-        # warm the plan pool: a burst of every shape, as a long-running server has
-        shapes = {}
-        for r in reqs:
-            shapes.setdefault((r[0].shape, r[2], r[3]), []).append(r)
-        warm = [srv.submit(*r) for v in shapes.values() for r in v[:4]]
-        for t in warm:
-            srv.wait(t)
+        nshapes = _warm(srv, reqs, warm_copies)
         for rate in rates:
-            gaps = np.random.default_rng(seed).exponential(1.0 / rate, count)
-            tickets = []
-            t0 = time.perf_counter()
-            arrival = t0
-            for r, g in zip(reqs, gaps):
-                arrival += g
-                while time.perf_counter() < arrival:
-                    pass
-                tickets.append(srv.submit(*r))
-            got = [srv.wait(t) for t in tickets]
-            span = time.perf_counter() - t0
-            lat = np.array([g["queue_ms"] + g["run_ms"] for g in got])
+            got, span = _serve(srv, reqs, rate, seed)
             same = same and all(a["makespan"] == b["makespan"] and np.array_equal(a["seq"], b["seq"])
                                 for a, b in zip(plain, got))
-            runs.append({"offered_per_s": rate, "solves_per_s": count / span,
-                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+            lat = _latency(got, solo_ms)
+            runs.append({"offered_per_s": rate, "solves_per_s": count / span, "p50_ms": lat["all"]["p50_ms"],
+                         "p99_ms": lat["all"]["p99_ms"], "latency": lat})
         st = srv.stats()
     best = max(runs, key=lambda x: x["solves_per_s"])
     return {"workload": f"{count} requests per rate, Poisson arrivals, n in {{15,20,30,50,100}}, m in "
-                        f"{{15,20}}, K in {{256,1024,4096}}, gpu-v2/clean modes, {inflight} slots",
+                        f"{{15,20}}, K in {{256,1024,4096}}, gpu-v2/clean modes, {inflight} slots, "
+                        f"{warm_copies} prepared plans per shape ({nshapes} shapes)",
             "solves_per_s": best["solves_per_s"], "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
             "rates": runs, "plain_solves_per_s": count / t_plain,
             "speedup_vs_plain": best["solves_per_s"] / (count / t_plain), "identical_results": same,
-            "plans_built": st["plans_built"], "plans_reused": st["plans_reused"],
-            "peak_inflight": st["peak_inflight"]}
+            "plans_built": st["plans_built"], "plans_prepared": st["plans_prepared"],
+            "plans_reused": st["plans_reused"], "peak_inflight": st["peak_inflight"]}
+
+
+def served_mixed_branching(ctx, device: int, count: int = 96, rate: float = 40.0, inflight: int = 96,
+                           seed: int = 7) -> dict:
+    """The served stream with mixed ICH/PMS branching: half the requests are BS-ICH / BS-PMS
+    (the CPU solvers' exact semantics: every ready op or the pivot machine's ops branched,
+    glibc rand(), serial bounded heap per request) at K=256, half gpu-v2 / clean at K in
+    {256, 1024, 4096}; n in {15, 20, 30, 50, 100}, m in {15, 20}.  The exact-semantics
+    requests stay at K=256 so that the plain one-at-a-time comparison finishes within the
+    bench's minutes (their heap is serial: a K=4096 100x20 BS-ICH search alone takes
+    seconds).  Plans are prepared for every shape first; results are compared with the
+    plain path."""
+    import random
+
+    import numpy as np
+
+    from beamsearch_jssp_gpu_gb300 import Server, synthetic_instance
+
+    rng = random.Random(seed)
+    reqs = []
+    for i in range(count):
+        n = rng.choice([15, 20, 30, 50, 100])
+        m = rng.choice([15, 20])
+        mode = rng.choice(["ich", "pms", "v2", "clean"])
+        K = 256 if mode in ("ich", "pms") else rng.choice([256, 1024, 4096])
+        mc, du = synthetic_instance(n, m, 30000 + i)
+        reqs.append((mc, du, mode, K, rng.randrange(1 << 30)))
+    plain, solo_ms, t_plain = _plain(ctx, reqs)
+    with Server(device, max_inflight=inflight) as srv:
+        nshapes = _warm(srv, reqs, 2)
+        got, span = _serve(srv, reqs, rate, seed)
+        st = srv.stats()
+    same = all(a["makespan"] == b["makespan"] and np.array_equal(a["seq"], b["seq"]) for a, b in zip(plain, got))
+    lat = _latency(got, solo_ms)
+    by_mode = {}
+    for md in ("ich", "pms", "v2", "clean"):
+        sel = [g for g, r in zip(got, reqs) if r[2] == md]
+        if sel:
+            x = np.array([g["queue_ms"] + g["run_ms"] for g in sel])
+            by_mode[md] = {"count": len(sel), "p50_ms": float(np.percentile(x, 50)),
+                           "p99_ms": float(np.percentile(x, 99))}
+    return {"workload": f"{count} requests, Poisson {rate:g}/s, ICH/PMS at K=256 and gpu-v2/clean at K in "
+                        f"{{256,1024,4096}}, n in {{15,20,30,50,100}}, m in {{15,20}}, {inflight} slots, "
+                        f"2 prepared plans per shape ({nshapes} shapes)",
+            "offered_per_s": rate, "solves_per_s": count / span, "p50_ms": lat["all"]["p50_ms"],
+            "p99_ms": lat["all"]["p99_ms"], "latency": lat, "by_mode": by_mode,
+            "plain_solves_per_s": count / t_plain, "speedup_vs_plain": t_plain / span,
+            "identical_results": same, "plans_built": st["plans_built"], "plans_reused": st["plans_reused"]}
 
 
 def k_sweep(args) -> int:
@@ -625,6 +731,9 @@ def main() -> int:
     ap.add_argument("--k-sweep", action="store_true", help="time vs beam width (20x15, gpu-v1), one line per K")
     ap.add_argument("--chunk-sweep", action="store_true",
                     help="ms per search of each k_step chunk size over a set of shapes (autotuner data)")
+    ap.add_argument("--step-form", type=int, default=None, choices=[0, 8, 16, 32, 1, 2],
+                    help="run the headline plan with this k_step form (0 = default rule; 8/16/32 warp per "
+                         "survivor; 1/2 thread per survivor) instead of autotuning it")
     ap.add_argument("--solve-times", action="store_true",
                     help="single gpu-v1/v2 searches (20x15 K=1024, 50x20 K=4096): ms per search")
     args = ap.parse_args()

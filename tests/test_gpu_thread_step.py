@@ -1,8 +1,10 @@
-"""The thread-per-survivor k_step forms against the oracle, bit for bit.
+"""The thread-per-survivor and lane-group k_step forms against the oracle, bit for bit.
 
 k_step_t materialises and expands one survivor per thread (forms 1: parent snapshots
-staged by 16-byte loads, word-interleaved by lane; 2: staged by bulk copies completing
-on an mbarrier).  Each is run over the parity suite's shapes -- every ready-list lane
+staged by word copies, interleaved by lane; 2: staged by bulk copies completing on an
+mbarrier); k_step_g gives each survivor a group of 4 lanes (forms 3, 4) or 8 lanes
+(forms 5, 6), staging by the group's 16-byte copies (3, 5) or one bulk copy (4, 6).
+Each is run over the parity suite's shapes -- every ready-list lane
 class up to n = 128, m = 1 (the jobs-chain quirk), K = 1, K not a multiple of 32 --
 with bounds that prune children and early levels where fewer children are scored than
 min(P*n, K), so that v2's filler ranks take both of their paths: a pruned child that is
@@ -13,7 +15,10 @@ import numpy as np
 import pytest
 
 from beamsearch_jssp_gpu_gb300 import BeamSpec, synthetic_instance
+from beamsearch_jssp_gpu_gb300 import _native as nat
 from oracle import oracle as O
+
+FORMS = nat.THREAD_FORMS + nat.GROUP_FORMS
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +41,7 @@ def _solve(ctx, mc, du, mode, K, seed, bk, form):
 
 def _check(ctx, mc, du, mode, K, seed, bk=500000):
     want = O.solve(mc, du, mode, K, seed, best_known=bk)
-    for form in (1, 2):
+    for form in FORMS:
         got = _solve(ctx, mc, du, mode, K, seed, bk, form)
         what = (form, mode, mc.shape, K, seed, bk)
         assert got["makespan"] == want["makespan"], what
@@ -64,15 +69,15 @@ def test_thread_forms_with_bounds(ctx, mode):
 
 
 def test_thread_form_in_a_batch_with_other_modes(ctx):
-    """A plan mixing modes: groups holding only v2/clean beams run the thread form, the
-    others the 32-survivor warp form; every beam equals its own solve."""
+    """A plan mixing modes: groups holding only v2/clean beams run the thread or group form,
+    the others the warp form of the same chunk size; every beam equals its own solve."""
     insts = [synthetic_instance(12, 4, 1), synthetic_instance(30, 6, 2), synthetic_instance(70, 3, 3)]
     beams = [BeamSpec(mode, K, 500000, 100 + i, i % 3, -1)
              for i, (mode, K) in enumerate([("v2", 64), ("clean", 100), ("v1", 50), ("ich", 16), ("v2", 33),
                                             ("pms", 8), ("clean", 257), ("v2", 512)])]
     plan = ctx.plan(insts, beams)
     try:
-        for form in (1, 2):
+        for form in FORMS:
             plan.chunk = form
             plan.run()
             for b, r in zip(beams, plan.results()):
