@@ -42,9 +42,8 @@ SELECT = {"force_large": 1, "no_large": 2, "no_direct": 4, "radix": 8, "no_dense
 ROUTE = {"large": 1, "direct": 2, "bucket": 4, "radix": 8, "dense": 16, "rank_lsd": 32, "raw_lsd": 64,
          "bitonic": 128}
 CHUNK_SIZES = (8, 16, 32)  # k_step work-unit sizes (survivors per thread block), warp per survivor
-THREAD_FORMS = (1, 2)      # k_step thread per survivor: word-copy / bulk-copy staging
-GROUP_FORMS = (3, 4, 5, 6)  # k_step lane group per survivor: 4 lanes (3, 4) / 8 lanes (5, 6), copy / bulk
-CHUNK_CANDIDATES = (0, 8, 16, 32, 1, 2, 3, 4, 5, 6)  # the autotuner's candidates: 0 = the default rule
+GROUP_FORMS = (1, 2, 3, 4)  # k_step lane group per survivor: 4 lanes copy/bulk (1, 2), 8 lanes copy/bulk (3, 4)
+CHUNK_CANDIDATES = (0, 8, 16, 32, 1, 2, 3, 4)  # the autotuner's candidates: 0 = the default rule
 
 
 class ServerConfig(ctypes.Structure):

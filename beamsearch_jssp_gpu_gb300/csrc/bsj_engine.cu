@@ -69,7 +69,7 @@ struct bsj_plan {
         int rule_var = 1;  // step variant (index into kStepVariant*) of the default rule
         int step_grid[kNumStepVariants] = {};
         bool has_v1 = false, has_gpu = false, has_compat = false;
-        bool thread_ok = false;  // every beam gpu-v2 / clean: thread-per-survivor k_step applies
+        bool group_ok = false;   // every beam gpu-v2 / clean: the lane-group k_step applies
     };
     std::vector<Group> groups;
     cudaEvent_t fork = nullptr;
@@ -212,18 +212,36 @@ int chunk_var_of(int chunk)
     return -1;
 }
 
+// Step variant (index into kStepVariant*) of a public chunk code; -1 if none.
+int step_var_of_code(int code)
+{
+    for (int v = 0; v < kNumStepVariants; v++)
+        if (kStepVariantCode[v] == code) return v;
+    return -1;
+}
+
 // Default rule for one beam group: `ranks` = survivors per level of the whole plan (all
 // groups run at once), `nq` = ceil(n/32) class holding most of the group's survivors,
-// `granks` = the group's own survivors per level.  Measured on GB300 (bench.py --chunk-sweep, gpu-v2,
-// 18 shapes from 10x5 K=256 to 100x20 8x4096; the rule picks the fastest on all): up to
-// 8 192 survivors per level the level is narrow and 8 per CTA spreads it over the most SMs
-// (3-30 % faster than 16), except for n > 64 at 4 096 and more, where per-CTA set-up
-// dominates and 32 wins; wider plans -- several beams at once -- run 16 per CTA (the
-// n <= 64 kernels with 16 and 32 keep six CTAs per SM resident), and 32 where the group
-// alone holds more than 8 192 (one wide beam, or several beams in lockstep: 8 beams of
-// 4 096 at 50x20 as 2 groups, 44.3 vs 49.5 ms) or n > 64.
-int rule_chunk_var(int64_t ranks, int nq, int64_t granks)
+// `granks` = the group's own survivors per level, `group_ok` = every beam of the group is
+// gpu-v2 / clean (the lane-group forms apply).  Measured on GB300 (bench.py --chunk-sweep,
+// gpu-v2, 18 shapes from 10x5 K=256 to 100x20 8x4096):
+//  - lane-group forms: 8 lanes per survivor (16 per CTA) wins every shape with more than
+//    2 048 survivors per level and n <= 64 (8 beams x 4 096 at 50x20: 32.3 vs 37.0 ms for
+//    the best warp form; 20x15 8x4 096: 8.0 vs 10.6 ms), except one group of more than
+//    8 192, where 4 lanes with a bulk copy win (K=16 384 at 20x15: 33.4 vs 35.8 ms); for
+//    n > 64 from 4 096 survivors on, 4 lanes with a bulk copy (100x20 8x4 096: 112.2 vs
+//    120.4 ms); narrower levels keep the 8-survivor warp form (single beams of K <= 1 024:
+//    3-15 % faster than the group forms);
+//  - other groups (v1, ICH/PMS): up to 8 192 survivors per level 8 per CTA, except n > 64
+//    at 4 096 and more, where 32 wins; wider plans 16 per CTA, and 32 where the group alone
+//    holds more than 8 192 or n > 64.
+int rule_chunk_var(int64_t ranks, int nq, int64_t granks, bool group_ok)
 {
+    if (group_ok) {
+        if (nq == 4) return ranks >= 4096 ? step_var_of_code(2) : chunk_var_of(8);
+        if (ranks <= 2048) return chunk_var_of(8);
+        return granks > 8192 ? step_var_of_code(2) : step_var_of_code(3);
+    }
     if (ranks <= 8192) return chunk_var_of((nq == 4 && ranks >= 4096) ? 32 : 8);
     return chunk_var_of((nq == 4 || granks > 8192) ? 32 : 16);
 }
@@ -512,22 +530,19 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             gr.args.seg_hi = hi;
             gr.args.rank_lo = p->prefix[lo];
             gr.args.rank_hi = p->prefix[hi];
-            gr.thread_ok = true;
+            gr.group_ok = true;
             for (int b = lo; b < hi; b++) {
                 const SegDesc& d = p->segs[b];
                 gr.maxN = std::max(gr.maxN, d.N);
                 gr.nq_mask |= 1 << d.nq;
                 if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
                 if (d.mode <= BSJ_MODE_CLEAN) gr.has_gpu = true; else gr.has_compat = true;
-                if (d.mode != BSJ_MODE_V2 && d.mode != BSJ_MODE_CLEAN) gr.thread_ok = false;
+                if (d.mode != BSJ_MODE_V2 && d.mode != BSJ_MODE_CLEAN) gr.group_ok = false;
             }
-            // k_step: one CTA per chunk (warp per survivor), one warp per 32-survivor chunk
-            // (thread per survivor)
+            // k_step: one CTA per chunk
             for (int v = 0; v < kNumStepVariants; v++) {
                 const int ci = chunk_var_of(kStepVariantChunk[v]);
                 int g = p->cprefix[ci][hi] - p->cprefix[ci][lo];
-                const int tv = kStepVariantThread[v];
-                if ((tv == 1 || tv == 2) && gr.thread_ok) g = (g + kTStepWarpsPerCta - 1) / kTStepWarpsPerCta;
                 gr.step_grid[v] = std::max(1, std::min(g, 65535));
             }
             const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
@@ -544,7 +559,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         int64_t per_nq[5] = {0, 0, 0, 0, 0};
         for (int b = gr.args.seg_lo; b < gr.args.seg_hi; b++) per_nq[p->segs[b].nq] += p->segs[b].K;
         const int nq = per_nq[4] > per_nq[2] && per_nq[4] > per_nq[1] ? 4 : (per_nq[2] > per_nq[1] ? 2 : 1);
-        gr.rule_var = rule_chunk_var(p->total_ranks, nq, per_nq[1] + per_nq[2] + per_nq[4]);
+        gr.rule_var = rule_chunk_var(p->total_ranks, nq, per_nq[1] + per_nq[2] + per_nq[4], gr.group_ok);
     }
     {
         const int v = tuned_chunk(ctx, p->shape);
@@ -567,7 +582,7 @@ StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
     const int lo = gr ? a.seg_lo : 0, hi = gr ? a.seg_hi : p->nseg;
     const int ci = chunk_var_of(kStepVariantChunk[v]);
     a.chunk = kStepVariantChunk[v];
-    a.thread_step = (gr && gr->thread_ok) ? kStepVariantThread[v] : 0;
+    a.group_step = (gr && gr->group_ok) ? kStepVariantGroup[v] : 0;
     a.select_force = p->select_force;
     a.chunk_prefix = p->d_cprefix + (size_t)ci * (p->nseg + 1);
     a.chunk_lo = p->cprefix[ci][lo];
@@ -1019,15 +1034,14 @@ bsj_status bsj_plan_set_chunk(bsj_plan* p, int32_t chunk)
 {
     if (!p) return BSJ_ERR_INVALID;
     if (chunk == 0) { p->variant = 0; return BSJ_OK; }
-    for (int v = 0; v < kNumStepVariants; v++) {
-        if (kStepVariantCode[v] == chunk) {
-            p->variant = 1 + v;
-            return BSJ_OK;
-        }
+    const int v = step_var_of_code(chunk);
+    if (v >= 0) {
+        p->variant = 1 + v;
+        return BSJ_OK;
     }
     return fail(p->ctx, BSJ_ERR_INVALID,
-                "chunk must be 0 (default rule), 8, 16, 32 (warp per survivor), 1, 2 (thread per survivor) "
-                "or 3, 4, 5, 6 (lane group per survivor)");
+                "chunk must be 0 (default rule), 8, 16, 32 (warp per survivor) or 1, 2, 3, 4 "
+                "(lane group per survivor)");
 }
 
 static_assert(BSJ_SELECT_FORCE_LARGE == kSelForceLarge && BSJ_SELECT_NO_LARGE == kSelNoLarge &&

@@ -547,31 +547,10 @@ __global__ void __launch_bounds__(kWarpsPerStepCta * 32) k_gather_v1(StepArgs a,
 }
 
 // ------------------------------------------------------------------------------------
-// k_step_t: materialise + expand with one THREAD per survivor (gpu-v2 / clean beams).
-//
-// The warp-per-survivor k_step spreads one survivor's ready list over the lanes, so most
-// lanes idle (a 50-job ready list is two lane-rounds, the pivot machine's candidates a
-// handful of lanes) and one survivor costs ~800 warp instructions.  Here a warp takes 32
-// consecutive ranks (one 32-rank key chunk), each lane one survivor end to end: load the
-// parent snapshot, apply the selected op, store the child, scan the child's ready list
-// for the pivot machine's ops, score them and emit the keys in slot order (a warp scan
-// of the per-lane key counts).  No block-wide barrier: the warps of a CTA are independent.
-//
-// Staging of the parent snapshot in shared memory, chosen per plan (StepArgs::thread_step):
-//   1  16-byte global loads, batched, stored word-interleaved by lane (word x of lane l at
-//      [x*32 + l]): every per-thread access of any field is bank-conflict free;
-//   2  one cp.async.bulk (TMA bulk copy, global -> shared, completion on a per-warp
-//      mbarrier) per lane, the snapshot kept contiguous (16-byte-aligned rows: 4-way bank
-//      conflicts on field access).
-// Result-identical to k_step (the same arithmetic in the same order per child).
+// Helpers of the lane-group k_step below: one survivor's snapshot in shared memory read
+// and written field by field, and the beam's layout held in registers.
 // ------------------------------------------------------------------------------------
-constexpr int kTStepWarps = kTStepWarpsPerCta;  // warps (32-rank chunks) per CTA
 constexpr uint32_t kTSpinLimit = 1u << 22;     // mbarrier try_wait attempts before giving up
-
-__host__ __device__ __forceinline__ size_t tstep_smem_bytes(int sb_max, int max_n)
-{
-    return (size_t)kTStepWarps * 32 * ((size_t)sb_max + (size_t)max_n);
-}
 
 // One lane's snapshot in shared memory: word x at w[x * XS].
 template <int XS>
@@ -598,51 +577,6 @@ struct TLay {
           off_nx(d.off_nx), hw(d.off_hdr >> 2), ops(all_ops + d.op_off) {}
     __device__ __forceinline__ uint32_t op(int j, int k) const { return __ldg(ops + j * m + k); }
 };
-
-// 16-byte loads of a snapshot into a lane's slot, four in flight at a time.
-template <int XS>
-__device__ __forceinline__ void tsnap_load(const TSnap<XS>& S, const uint8_t* src, int w16)
-{
-    const uint4* s4 = reinterpret_cast<const uint4*>(src);
-    int q = 0;
-    for (; q + 4 <= w16; q += 4) {
-        uint4 v[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) v[u] = __ldg(s4 + q + u);
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            S.set_word(4 * (q + u) + 0, v[u].x);
-            S.set_word(4 * (q + u) + 1, v[u].y);
-            S.set_word(4 * (q + u) + 2, v[u].z);
-            S.set_word(4 * (q + u) + 3, v[u].w);
-        }
-    }
-    for (; q < w16; q++) {
-        const uint4 v = __ldg(s4 + q);
-        S.set_word(4 * q + 0, v.x);
-        S.set_word(4 * q + 1, v.y);
-        S.set_word(4 * q + 2, v.z);
-        S.set_word(4 * q + 3, v.w);
-    }
-}
-
-// Asynchronous word copies of a snapshot into a lane's interleaved slot: every copy in
-// flight at once (one memory round trip); the caller commits and waits.
-__device__ __forceinline__ void tsnap_copy_async(uint32_t* w_il, const uint8_t* src, int words)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(w_il);
-    for (int x = 0; x < words; x++)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa + 128u * (unsigned)x), "l"(src + 4 * x)
-                     : "memory");
-}
-
-template <int XS>
-__device__ __forceinline__ void tsnap_store(const TSnap<XS>& S, uint8_t* dst, int w16)
-{
-    uint4* d4 = reinterpret_cast<uint4*>(dst);
-    for (int q = 0; q < w16; q++)
-        d4[q] = make_uint4(S.word(4 * q), S.word(4 * q + 1), S.word(4 * q + 2), S.word(4 * q + 3));
-}
 
 // Job-predecessor finish (pred_finish above, on a lane's snapshot).
 template <int XS>
@@ -673,252 +607,6 @@ __device__ int tnth_candidate(const TSnap<XS>& S, const TLay& L, uint32_t seed_t
         }
     }
     return -1;
-}
-
-template <int MODE_T>
-__global__ void __launch_bounds__(kTStepWarps * 32) k_step_t(StepArgs a, int s)
-{
-    constexpr bool BULK = (MODE_T == 2);
-    constexpr int XS = BULK ? 1 : 32;
-    extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ __align__(8) unsigned long long s_mbar[kTStepWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sw = a.sb_max >> 2;   // words per snapshot slot
-    uint32_t* wbase = reinterpret_cast<uint32_t*>(smem) + (size_t)warp * 32 * sw;
-    TSnap<XS> S;
-    S.w = BULK ? wbase + (size_t)lane * sw : wbase + lane;
-    // candidate positions of this lane's expansion: entry b at posl[b * 32]
-    uint8_t* posl = smem + (size_t)kTStepWarps * 32 * a.sb_max + (size_t)warp * 32 * a.max_n + lane;
-    pdl_trigger();
-    if (BULK) {
-        if (lane == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&s_mbar[warp])), "r"(32) : "memory");
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        __syncwarp();
-    }
-    uint32_t phase = 0;
-    pdl_wait();
-    for (int chunk = a.chunk_lo + blockIdx.x * kTStepWarps + warp; chunk < a.chunk_hi;
-         chunk += gridDim.x * kTStepWarps) {
-        const int seg = find_seg(a.chunk_prefix, a.seg_lo, a.seg_hi, chunk);
-        const SegDesc& d = a.segs[seg];
-        if (s >= d.N - 1) continue;   // the same for the whole warp (one chunk)
-        SegState& st = a.st[seg];
-        if (d.mode != MODE_V2 && d.mode != MODE_CLEAN) {   // the host runs only these beams here
-            if (lane == 0) atomicOr(&st.status, kStatusBadSelect);
-            continue;
-        }
-        const TLay L(d, a.ops);
-        const int mode = d.mode, K = d.K, words = d.words, group = d.group;
-        const uint32_t seed = d.seed;
-        const int q = chunk - __ldg(a.chunk_prefix + seg);
-        const int P = (s < 0) ? 1 : *((volatile int32_t*)&st.P);
-        const int n = L.n, m = L.m, w16 = L.sbytes >> 4;
-        const int r = q * 32 + lane;
-        const bool act = r < P;
-        uint8_t* childbuf = a.beam_pool + d.beam_off[(s + 1) & 1];
-        const uint8_t* parent = a.beam_pool + d.beam_off[s & 1];
-        const uint8_t* pos_in = a.pos_pool + d.pos_off[s & 1];
-        uint8_t* pos_out = a.pos_pool + d.pos_off[(s + 1) & 1];
-        uint32_t* hist = a.hist + d.hist_off + (int64_t)(s < 0 ? 0 : s) * K;
-        uint32_t* masks = a.masks + d.mask_off;
-        unsigned long long* kdst0 = a.keys + d.key_off + (int64_t)q * 32 * n;
-        int32_t* kcnt = a.kcnt + d.kcnt_off + q;
-        const int bound = st.bound;
-
-        // ---- 1. the source snapshot of this rank
-        uint32_t e = 0;
-        int c = 0, b = 0, ii = -1;
-        if (act && s >= 0) {
-            e = __ldg(a.sel + d.sel_off + r);
-            const uint32_t slot = e & ~kFillerFlag;
-            c = (int)(slot / (uint32_t)n);
-            b = (int)slot - c * n;
-        }
-        if (BULK) {
-            const uint32_t bar = smem_u32(&s_mbar[warp]);
-            if (act && s >= 0) {
-                // the slot was last written through the generic proxy: order that before
-                // the bulk copy's (async-proxy) write
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
-                             ::"r"(bar), "r"(L.sbytes) : "memory");
-                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                             ::"r"(smem_u32(S.w)), "l"(parent + (int64_t)c * L.sbytes), "r"(L.sbytes), "r"(bar)
-                             : "memory");
-            } else {
-                asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar)
-                             : "memory");
-            }
-            if (act && s >= 0 && !(e & kFillerFlag)) ii = __ldg(pos_in + (e & ~kFillerFlag));
-            uint32_t done = 0;
-            for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
-                asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                             " selp.u32 %0, 1, 0, p;\n}\n"
-                             : "=r"(done) : "r"(bar), "r"(phase) : "memory");
-            }
-            phase ^= 1u;
-            if (!__all_sync(FULL_MASK, done)) {
-                // a copy that never completed: flag it, wait once more (bounded) for the
-                // warp's copies, and stop working on this launch
-                if (lane == 0) atomicOr(&st.status, kStatusBadSelect);
-                for (uint32_t it = 0; it < kTSpinLimit && !done; it++) {
-                    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                                 " selp.u32 %0, 1, 0, p;\n}\n"
-                                 : "=r"(done) : "r"(bar), "r"(phase ^ 1u) : "memory");
-                }
-                return;
-            }
-        } else {
-            if (act && s >= 0) {
-                tsnap_copy_async(S.w, parent + (int64_t)c * L.sbytes, L.sbytes >> 2);
-                if (!(e & kFillerFlag)) ii = __ldg(pos_in + (e & ~kFillerFlag));
-            }
-            cp_async_commit();
-            cp_async_wait_all();
-        }
-
-        // ---- 2. materialise (v2: kernel_materialize_topk, gpu/v2_twophases/solver.cu:193-252)
-        uint32_t hist_val = kMark;
-        if (act && s < 0) {
-            for (int x = 0; x < (L.sbytes >> 2); x++) S.set_word(x, 0u);
-            for (int j = 0; j < n; j++) S.set_byte(L.off_rd + j, j);
-            S.set_word(L.hw, (uint32_t)n);
-            S.set_word(L.hw + 2, kMark);
-            tsnap_store<XS>(S, childbuf, w16);
-        } else if (act) {
-            if (e & kFillerFlag) ii = tnth_candidate<XS>(S, L, seed + (uint32_t)s, c, b);
-            if (ii >= 0) {
-                const uint32_t h0 = S.word(L.hw);
-                const int r0 = (int)(h0 & 0xFFFFu), ns = (int)(h0 >> 16);
-                const int j = S.byte(L.off_rd + ii);
-                const int k = S.byte(L.off_nx + j);
-                const uint32_t o = L.op(j, k);
-                const int mc = (int)(o & 0xFFu);
-                const int pred = tpred_finish<XS>(S, L, j, k);
-                const int trv = (int)S.word(mc);
-                const int fin = (trv > pred ? trv : pred) + (int)(o >> 8);
-                const int lastj = S.byte(L.off_rd + r0 - 1);
-                const bool cont = (k + 1 < m);
-                const int cm = (int)S.word(L.hw + 1);
-                S.set_word(mc, (uint32_t)fin);
-                S.set_word(L.off_jr4 + j, (uint32_t)fin);
-                if (ii != r0 - 1) S.set_byte(L.off_rd + ii, lastj);
-                if (cont) S.set_byte(L.off_rd + r0 - 1, j);
-                S.set_byte(L.off_nx + j, k + 1);
-                S.set_word(L.hw, ((uint32_t)(ns + 1) << 16) | (uint32_t)(r0 - 1 + (cont ? 1 : 0)));
-                S.set_word(L.hw + 1, (uint32_t)(cm > fin ? cm : fin));
-                hist_val = ((uint32_t)c << 8) | (uint32_t)j;
-                S.set_word(L.hw + 2, hist_val);
-                S.set_word(L.hw + 3, (uint32_t)(s + 1));
-                tsnap_store<XS>(S, childbuf + (int64_t)r * L.sbytes, w16);
-            } else {
-                // filler rank whose branch does not exist: v2 leaves the ping-pong slot as
-                // it was (gpu/v2_twophases/solver.cu:191) and expands what it holds
-                if (mode == MODE_CLEAN) atomicOr(&st.status, kStatusBadSelect);
-                tsnap_load<XS>(S, childbuf + (int64_t)r * L.sbytes, w16);
-            }
-            hist[r] = hist_val;
-        }
-
-        // ---- 3. expand for level t (kernel_score_candidates, gpu/v2_twophases/solver.cu:68-123)
-        const int t = s + 1;
-        const uint32_t seed_t = seed + (uint32_t)t;
-        const bool lastlv = (t == L.N - 1);
-        int cnt = 0, trp = 0, pcmax = 0, ns1 = 1;
-        uint32_t vm0 = 0u, vm1 = 0u, vm2 = 0u, vm3 = 0u;
-        const int rr = act ? (int)(S.word(L.hw) & 0xFFFFu) : 0;
-        if (rr > 0) {
-            const uint32_t h0 = S.word(L.hw);
-            ns1 = (int)(h0 >> 16) + 1;
-            pcmax = (int)S.word(L.hw + 1);
-            const uint32_t h = pivot_hash(seed_t + (uint32_t)r);
-            const int jp = S.byte(L.off_rd + (int)(h % (uint32_t)rr));
-            const int pm = (int)(L.op(jp, S.byte(L.off_nx + jp)) & 0xFFu);
-            trp = (int)S.word(pm);
-            uint8_t* prow = pos_out + (int64_t)r * n;
-            const bool rows = t < L.N - 1;
-            for (int i0 = 0; i0 < rr; i0 += 4) {
-                // off_rd = 4m + 4n is a multiple of 4: ready positions i0..i0+3 share a word
-                const uint32_t w4 = S.word((L.off_rd + i0) >> 2);
-                uint32_t ou[4];
-                int ju[4], ku[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    ju[u] = (int)((w4 >> (8 * u)) & 0xFFu);
-                    ku[u] = 0;
-                    ou[u] = 0xFFu;
-                    if (i0 + u < rr) {
-                        ku[u] = S.byte(L.off_nx + ju[u]);
-                        ou[u] = L.op(ju[u], ku[u]);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (i0 + u < rr && (int)(ou[u] & 0xFFu) == pm) {
-                        const int pred = tpred_finish<XS>(S, L, ju[u], ku[u]);
-                        const int fin = (trp > pred ? trp : pred) + (int)(ou[u] >> 8);
-                        const int cmx = pcmax > fin ? pcmax : fin;
-                        if (cmx < bound) {   // gpu/v1/solver.cu:120
-                            const uint32_t bit = 1u << (cnt & 31);
-                            const int wq = cnt >> 5;
-                            vm0 |= (wq == 0) ? bit : 0u;
-                            vm1 |= (wq == 1) ? bit : 0u;
-                            vm2 |= (wq == 2) ? bit : 0u;
-                            vm3 |= (wq == 3) ? bit : 0u;
-                        }
-                        posl[cnt * 32] = (uint8_t)(i0 + u);
-                        if (rows) prow[cnt] = (uint8_t)(i0 + u);
-                        cnt++;
-                    }
-                }
-            }
-        }
-        const int nv = __popc(vm0) + __popc(vm1) + __popc(vm2) + __popc(vm3);
-        // slot order inside the chunk: ranks ascending, branches ascending
-        int pre = nv;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(FULL_MASK, pre, o);
-            if (lane >= o) pre += y;
-        }
-        const int total = __shfl_sync(FULL_MASK, pre, 31);
-        pre -= nv;
-        if (act) {
-#pragma unroll
-            for (int w = 0; w < 4; w++)
-                if (w < words) masks[(int64_t)r * words + w] = w == 0 ? vm0 : (w == 1 ? vm1 : (w == 2 ? vm2 : vm3));
-        }
-        if (nv > 0) {
-            unsigned long long* kdst = kdst0 + pre;
-            const float fns = __int2float_rn(ns1);
-            int o_k = 0;
-            for (int bb = 0; bb < cnt; bb++) {
-                const uint32_t vw = (bb >> 5) == 0 ? vm0 : ((bb >> 5) == 1 ? vm1 : ((bb >> 5) == 2 ? vm2 : vm3));
-                if (!((vw >> (bb & 31)) & 1u)) continue;
-                const int i = posl[bb * 32];
-                const int j = S.byte(L.off_rd + i);
-                const int k = S.byte(L.off_nx + j);
-                const uint32_t o = L.op(j, k);
-                const int pred = tpred_finish<XS>(S, L, j, k);
-                const int fin = (trp > pred ? trp : pred) + (int)(o >> 8);
-                const int cmx = pcmax > fin ? pcmax : fin;
-                const float base = __fdiv_rn(__int2float_rn(cmx), fns);
-                const uint32_t ni = noise_hash(seed_t, (uint32_t)r, (uint32_t)bb) % 1000u;
-                const float sc = __fadd_rn(base, __ldg(a.noise + ni));
-                const uint32_t slot = (uint32_t)(r * n + bb);
-                kdst[o_k++] = ((unsigned long long)__float_as_uint(sc) << 32) | slot;
-                if (lastlv && ns1 == L.N) {
-                    atomicMin(&st.best, ((unsigned long long)(uint32_t)cmx << 32) |
-                                            ((unsigned long long)slot << 8) | (uint32_t)j);
-                    atomicMin(a.group_best + group, cmx);
-                }
-            }
-        }
-        if (lane == 0) *kcnt = total;
-        __syncwarp();
-    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -3014,14 +2702,6 @@ static cudaError_t for_each_step(F&& f)
 }
 
 template <typename F>
-static cudaError_t for_each_tstep(F&& f)
-{
-    cudaError_t e = f(k_step_t<1>);
-    if (e == cudaSuccess) e = f(k_step_t<2>);
-    return e;
-}
-
-template <typename F>
 static cudaError_t for_each_gstep(F&& f)
 {
     cudaError_t e = f(k_step_g<4, 1>, 4);
@@ -3042,8 +2722,6 @@ static cudaError_t set_carveout()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
-    if (e == cudaSuccess)
-        e = for_each_tstep([&](auto fn) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess)
         e = for_each_gstep([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gather_v1, cudaFuncAttributePreferredSharedMemoryCarveout, c);
@@ -3074,7 +2752,6 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
-    if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
     if (e == cudaSuccess)
         e = for_each_gstep([&](auto fn, int g) { return raise_smem(fn, gstep_smem_bytes(g, sb_max, max_n)); });
     return e;
@@ -3086,7 +2763,6 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
-    if (e == cudaSuccess) e = for_each_tstep([&](auto fn) { return raise_smem(fn, tstep_smem_bytes(sb_max, max_n)); });
     if (e == cudaSuccess)
         e = for_each_gstep([&](auto fn, int g) { return raise_smem(fn, gstep_smem_bytes(g, sb_max, max_n)); });
     return e;
@@ -3131,26 +2807,18 @@ static cudaError_t launch_step_ch(const StepArgs& a, int s, int grid, int nq_mas
 
 cudaError_t launch_step(const StepArgs& a, int s, int grid, int nq_mask, cudaStream_t stream)
 {
-    if (a.thread_step >= 3) {
-        const int G = a.thread_step <= 4 ? 4 : 8;
+    if (a.group_step) {
+        const int G = a.group_step <= 2 ? 4 : 8;
         if (a.chunk != kGStepWarps * (32 / G)) return cudaErrorInvalidValue;
         const size_t sm = gstep_smem_bytes(G, a.sb_max, a.max_n);
         const int block = kGStepWarps * 32;
-        switch (a.thread_step) {
-        case 3: return launch_kernel(k_step_g<4, 1>, grid, block, sm, stream, s >= 0, a, s);
-        case 4: return launch_kernel(k_step_g<4, 2>, grid, block, sm, stream, s >= 0, a, s);
-        case 5: return launch_kernel(k_step_g<8, 1>, grid, block, sm, stream, s >= 0, a, s);
-        case 6: return launch_kernel(k_step_g<8, 2>, grid, block, sm, stream, s >= 0, a, s);
+        switch (a.group_step) {
+        case 1: return launch_kernel(k_step_g<4, 1>, grid, block, sm, stream, s >= 0, a, s);
+        case 2: return launch_kernel(k_step_g<4, 2>, grid, block, sm, stream, s >= 0, a, s);
+        case 3: return launch_kernel(k_step_g<8, 1>, grid, block, sm, stream, s >= 0, a, s);
+        case 4: return launch_kernel(k_step_g<8, 2>, grid, block, sm, stream, s >= 0, a, s);
         default: return cudaErrorInvalidValue;
         }
-    }
-    if (a.thread_step) {
-        if (a.chunk != 32) return cudaErrorInvalidValue;
-        const size_t sm = tstep_smem_bytes(a.sb_max, a.max_n);
-        const int block = kTStepWarps * 32;
-        if (a.thread_step == 1) return launch_kernel(k_step_t<1>, grid, block, sm, stream, s >= 0, a, s);
-        if (a.thread_step == 2) return launch_kernel(k_step_t<2>, grid, block, sm, stream, s >= 0, a, s);
-        return cudaErrorInvalidValue;
     }
     switch (a.chunk) {
     case 8: return launch_step_ch<8>(a, s, grid, nq_mask, stream);

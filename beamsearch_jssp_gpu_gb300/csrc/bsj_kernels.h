@@ -27,8 +27,8 @@ struct StepArgs {
     int32_t rank_lo, rank_hi;
     int32_t chunk;                // ranks per k_step CTA (one of kChunkSizes)
     int32_t select_force;         // kSel* route flags for k_select (0 = by level size)
-    int32_t thread_step;          // k_step form: 0 warp per survivor; 1 / 2 thread per survivor
-                                  // (k_step_t, chunk 32) with load / bulk-copy staging
+    int32_t group_step;           // k_step form: 0 warp per survivor; 1-4 a lane group per
+                                  // survivor (k_step_g: 4 lanes copy / bulk, 8 lanes copy / bulk)
     uint8_t* beam_pool;
     uint8_t* slot_pool;
     unsigned long long* keys;
@@ -44,18 +44,16 @@ struct StepArgs {
     const double* dnoise;         // [1000]: (double)k / 1e6 (BS-PMS noise), IEEE round-to-nearest
 };
 
-// k_step variants (the autotuner's candidates besides the default rule): warp per
-// survivor with 8, 16 or 32 survivors per CTA; one thread per survivor (32 per warp, key
-// chunks of 32) with the parent snapshots staged by word copies or by bulk copies; a group
-// of 4 lanes per survivor (32 per CTA) or of 8 lanes (16 per CTA), parents staged by the
-// group's 16-byte copies or by one bulk copy.  Thread and group variants apply to beam
-// groups whose beams are all gpu-v2 / clean; other groups run the warp kernel with the
-// same chunk size.  Public codes (bsj_plan_set_chunk): 8, 16, 32, 1, 2, 3, 4, 5, 6.
-constexpr int kNumStepVariants = 9;
-constexpr int kStepVariantChunk[kNumStepVariants] = {8, 16, 32, 32, 32, 32, 32, 16, 16};
-constexpr int kStepVariantThread[kNumStepVariants] = {0, 0, 0, 1, 2, 3, 4, 5, 6};
-constexpr int kStepVariantCode[kNumStepVariants] = {8, 16, 32, 1, 2, 3, 4, 5, 6};
-constexpr int kTStepWarpsPerCta = 4;   // k_step_t: warps (32-survivor chunks) per CTA
+// k_step variants (the autotuner's candidates besides the default rule): a warp per
+// survivor with 8, 16 or 32 survivors per CTA; a group of 4 lanes per survivor (32 per
+// CTA) or of 8 lanes (16 per CTA), the parent snapshots staged by the group's 16-byte
+// copies or by one bulk copy.  Group variants apply to beam groups whose beams are all
+// gpu-v2 / clean; other groups run the warp kernel with the same chunk size.  Public
+// codes (bsj_plan_set_chunk): 8, 16, 32 (warp), 1, 2, 3, 4 (group).
+constexpr int kNumStepVariants = 7;
+constexpr int kStepVariantChunk[kNumStepVariants] = {8, 16, 32, 32, 32, 16, 16};
+constexpr int kStepVariantGroup[kNumStepVariants] = {0, 0, 0, 1, 2, 3, 4};
+constexpr int kStepVariantCode[kNumStepVariants] = {8, 16, 32, 1, 2, 3, 4};
 
 // k_heap launch configuration: the largest K, child-table row (bytes) and n of the
 // launch's ICH/PMS beams, and the parents prepared per chunk.

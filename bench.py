@@ -731,9 +731,9 @@ def main() -> int:
     ap.add_argument("--k-sweep", action="store_true", help="time vs beam width (20x15, gpu-v1), one line per K")
     ap.add_argument("--chunk-sweep", action="store_true",
                     help="ms per search of each k_step chunk size over a set of shapes (autotuner data)")
-    ap.add_argument("--step-form", type=int, default=None, choices=[0, 8, 16, 32, 1, 2],
+    ap.add_argument("--step-form", type=int, default=None, choices=[0, 8, 16, 32, 1, 2, 3, 4],
                     help="run the headline plan with this k_step form (0 = default rule; 8/16/32 warp per "
-                         "survivor; 1/2 thread per survivor) instead of autotuning it")
+                         "survivor; 1-4 lane group per survivor) instead of autotuning it")
     ap.add_argument("--solve-times", action="store_true",
                     help="single gpu-v1/v2 searches (20x15 K=1024, 50x20 K=4096): ms per search")
     args = ap.parse_args()

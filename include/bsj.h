@@ -192,16 +192,17 @@ bsj_status bsj_plan_select_routes(bsj_plan *plan, uint32_t *routes);
 
 /* ---- Autotuning (no counterpart in the reference, whose launch shape is fixed:
    one block of n threads per parent, gpu/v1/solver.cu:186,237) ----
-   The materialise+expand kernel has five forms ("chunk" codes), and which is fastest
+   The materialise+expand kernel has seven forms ("chunk" codes), and which is fastest
    depends on n, m, K and the number of beams; results never depend on it:
      8, 16, 32   a warp per survivor (the ready list spread over the lanes), 8, 16 or 32
                  consecutive survivors per thread block: small chunks spread a narrow level
                  over more SMs, large ones amortise per-block work;
-     1, 2        a thread per survivor, 32 consecutive survivors per warp (far fewer
-                 instructions per survivor; gpu-v2 / clean beams only -- other beams of
-                 the group run the 32-survivor warp form): the parent snapshots are
-                 staged in shared memory by 16-byte loads (1) or by bulk copies with an
-                 mbarrier (2).
+     1, 2, 3, 4  a group of lanes per survivor (gpu-v2 / clean beams only -- other beams of
+                 the group run the warp form of the same chunk): 4 lanes, 32 survivors per
+                 block (1, 2) or 8 lanes, 16 per block (3, 4); the parent snapshots staged in
+                 shared memory by the group's 16-byte copies (1, 3) or by one bulk copy with
+                 an mbarrier (2, 4).  Several times fewer instructions per survivor than the
+                 warp form, so beams running side by side contend less.
    Each beam group of a plan (a graph branch) has its own form.  Candidates: 0 = the
    default rule (per group, from the plan's survivors per level, the group's n and
    modes), and each code above for every group.
@@ -209,14 +210,14 @@ bsj_status bsj_plan_select_routes(bsj_plan *plan, uint32_t *routes);
    its graph, then `repeats` timed runs on `stream`, synchronously), keeps the fastest,
    and records it in a process-wide table keyed by device and batch shape, so later plans
    of the same shape (any context, the server included) start with it.  ms (may be NULL)
-   receives the mean ms per run of each candidate in the order 0, 8, 16, 32, 1, 2 (six
-   floats; a form equal to what the rule gives every group is not run again: its entry
-   repeats the rule's); *chunk (may be NULL) the choice.  The plan's results afterwards
+   receives the mean ms per run of each candidate in the order 0, 8, 16, 32, 1, 2, 3, 4
+   (eight floats; a form equal to what the rule gives every group is not run again: its
+   entry repeats the rule's); *chunk (may be NULL) the choice.  The plan's results afterwards
    are those of a complete run.  Plans start with the tuned candidate of their shape if
    there is one, else the rule.  bsj_plan_set_chunk selects a candidate; bsj_plan_chunk
    returns it.
    bsj_set_autotune: with enable != 0, bsj_solve_batch / bsj_solve tune every batch shape
-   they have not seen on this device before its first solve (about 6 extra solves once
+   they have not seen on this device before its first solve (about 8 extra solves once
    per shape). */
 bsj_status bsj_plan_autotune(bsj_plan *plan, void *stream, int32_t repeats, int32_t *chunk, float *ms);
 bsj_status bsj_plan_set_chunk(bsj_plan *plan, int32_t chunk);

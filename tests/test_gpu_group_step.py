@@ -1,10 +1,8 @@
-"""The thread-per-survivor and lane-group k_step forms against the oracle, bit for bit.
+"""The lane-group k_step forms against the oracle, bit for bit.
 
-k_step_t materialises and expands one survivor per thread (forms 1: parent snapshots
-staged by word copies, interleaved by lane; 2: staged by bulk copies completing on an
-mbarrier); k_step_g gives each survivor a group of 4 lanes (forms 3, 4) or 8 lanes
-(forms 5, 6), staging by the group's 16-byte copies (3, 5) or one bulk copy (4, 6).
-Each is run over the parity suite's shapes -- every ready-list lane
+k_step_g materialises and expands each survivor with a group of 4 lanes (forms 1, 2) or
+8 lanes (forms 3, 4), the parent snapshot staged in shared memory by the group's 16-byte
+copies (1, 3) or by one bulk copy completing on an mbarrier (2, 4).  Each is run over the parity suite's shapes -- every ready-list lane
 class up to n = 128, m = 1 (the jobs-chain quirk), K = 1, K not a multiple of 32 --
 with bounds that prune children and early levels where fewer children are scored than
 min(P*n, K), so that v2's filler ranks take both of their paths: a pruned child that is
@@ -18,7 +16,7 @@ from beamsearch_jssp_gpu_gb300 import BeamSpec, synthetic_instance
 from beamsearch_jssp_gpu_gb300 import _native as nat
 from oracle import oracle as O
 
-FORMS = nat.THREAD_FORMS + nat.GROUP_FORMS
+FORMS = nat.GROUP_FORMS
 
 pytestmark = pytest.mark.gpu
 
@@ -54,23 +52,24 @@ def _check(ctx, mc, du, mode, K, seed, bk=500000):
 
 @pytest.mark.parametrize("mode", ["v2", "clean"])
 @pytest.mark.parametrize("n,m,K,iseed", SHAPES)
-def test_thread_forms_match_oracle(ctx, mode, n, m, K, iseed):
+def test_group_forms_match_oracle(ctx, mode, n, m, K, iseed):
     mc, du = synthetic_instance(n, m, iseed)
     for seed in (0, 2**32 - 2 - iseed):
         _check(ctx, mc, du, mode, K, seed)
 
 
 @pytest.mark.parametrize("mode", ["v2", "clean"])
-def test_thread_forms_with_bounds(ctx, mode):
+def test_group_forms_with_bounds(ctx, mode):
     mc, du = synthetic_instance(10, 5, 21)
     base = O.solve(mc, du, mode, 64, 3)["makespan"]
     for bk in (base + 30, base + 1, base, base - 20, 1):
         _check(ctx, mc, du, mode, 64, 3, bk)
 
 
-def test_thread_form_in_a_batch_with_other_modes(ctx):
-    """A plan mixing modes: groups holding only v2/clean beams run the thread or group form,
-    the others the warp form of the same chunk size; every beam equals its own solve."""
+def test_group_form_in_a_batch_with_other_modes(ctx):
+    """A plan mixing modes and instances: beam groups holding only v2/clean beams run the
+    lane-group form, the others the warp form of the same chunk size; every beam equals its
+    own oracle solve."""
     insts = [synthetic_instance(12, 4, 1), synthetic_instance(30, 6, 2), synthetic_instance(70, 3, 3)]
     beams = [BeamSpec(mode, K, 500000, 100 + i, i % 3, -1)
              for i, (mode, K) in enumerate([("v2", 64), ("clean", 100), ("v1", 50), ("ich", 16), ("v2", 33),
