@@ -100,3 +100,12 @@ def test_large_levels_match_oracle(ctx, mode, n, m, K):
     level here), which run the chunk-walking select with 32-bit dense-rank keys."""
     mc, du = synthetic_instance(n, m, 3)
     check(ctx, mc, du, mode, K, 5)
+
+
+@pytest.mark.parametrize("mode", ["ich", "pms"])
+@pytest.mark.parametrize("K", [8192, 9000])
+def test_wide_heaps_match_oracle(ctx, mode, K):
+    """ICH/PMS beams whose bounded heap fills to K=8192 and K=9000 (4-5 M children offered
+    over 60 levels): the replay of libstdc++'s heap steps stays exact at these widths."""
+    mc, du = synthetic_instance(12, 5, 3)
+    check(ctx, mc, du, mode, K, 77)
