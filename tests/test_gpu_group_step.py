@@ -87,3 +87,17 @@ def test_group_form_in_a_batch_with_other_modes(ctx):
                 assert r["expanded"] == want["expanded"], (form, b)
     finally:
         plan.close()
+
+
+@pytest.mark.parametrize("mode", ["v2", "clean"])
+def test_group_forms_wide_beam(ctx, mode):
+    """K=16384 on 16x3 (~100 K candidate keys per level: the large-level select) with each
+    group form against the oracle."""
+    mc, du = synthetic_instance(16, 3, 3)
+    want = O.solve(mc, du, mode, 16384, 0)
+    for form in FORMS:
+        got = _solve(ctx, mc, du, mode, 16384, 0, 500000, form)
+        what = (form, mode)
+        assert got["makespan"] == want["makespan"], what
+        assert np.array_equal(got["seq"], want["seq"]), what
+        assert got["expanded"] == want["expanded"] and got["slots"] == want["slots"], what
