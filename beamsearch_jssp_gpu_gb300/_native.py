@@ -38,9 +38,9 @@ EXPORTED = [
 ]
 # top-K selection routes (include/bsj.h BSJ_SELECT_* / BSJ_ROUTE_*)
 SELECT = {"force_large": 1, "no_large": 2, "no_direct": 4, "radix": 8, "no_dense": 16, "rank_lsd": 32,
-          "bitonic": 64}
+          "bitonic": 64, "no_cluster": 128, "force_cluster": 256}
 ROUTE = {"large": 1, "direct": 2, "bucket": 4, "radix": 8, "dense": 16, "rank_lsd": 32, "raw_lsd": 64,
-         "bitonic": 128}
+         "bitonic": 128, "cluster": 256}
 CHUNK_SIZES = (8, 16, 32)  # k_step work-unit sizes (survivors per thread block), warp per survivor
 GROUP_FORMS = (1, 2, 3, 4)  # k_step lane group per survivor: 4 lanes copy/bulk (1, 2), 8 lanes copy/bulk (3, 4)
 CHUNK_CANDIDATES = (0, 8, 16, 32, 1, 2, 3, 4)  # the autotuner's candidates: 0 = the default rule

@@ -64,10 +64,20 @@ constexpr int kSelForceRadix = 8;   // MSD radix select of the R-th key, not the
 constexpr int kSelNoDense = 16;     // LSD passes on the raw score bits (no dense ranks)
 constexpr int kSelRankLsd = 32;     // dense ranks written into the keys, then LSD passes
 constexpr int kSelBitonic = 64;     // block bitonic sort of the survivors
-constexpr int kSelAll = 127;
+constexpr int kSelNoCluster = 128;  // one CTA per beam (no cluster select launch)
+constexpr int kSelForceCluster = 256;  // cluster launch, and its route on every level it can take
+constexpr int kSelAll = 511;
 // Routes the levels of a beam took (SegState::select_paths, OR over the levels).
 constexpr uint32_t kPathLarge = 1, kPathDirect = 2, kPathBucket = 4, kPathRadix = 8, kPathDense = 16,
-                   kPathRankLsd = 32, kPathRawLsd = 64, kPathBitonic = 128;
+                   kPathRankLsd = 32, kPathRawLsd = 64, kPathBitonic = 128, kPathCluster = 256;
+// CTAs of one beam's cluster select, the smallest beam width it is launched for, and the
+// smallest level (candidate keys) its route takes.  Measured on GB300 (ms per search,
+// cluster / one block): 50x20 K=4096 25.5 / 28.3, 20x15 K=4096 6.97 / 7.37, 100x20 K=4096
+// 69.5 / 100.1; taking only levels above 8 192 keys was slower on every shape, and
+// launching it for K=2048 at 20x15 (levels of ~4.5 K keys) slower than one block.
+constexpr int kSelectCluster = 2;
+constexpr int kSelectClusterMinK = 4096;
+constexpr int kClusterMinKeys = 4096;
 
 struct SegDesc {
     int32_t n, m, N, K;

@@ -70,6 +70,8 @@ struct bsj_plan {
         int step_grid[kNumStepVariants] = {};
         bool has_v1 = false, has_gpu = false, has_compat = false;
         bool group_ok = false;   // every beam gpu-v2 / clean: the lane-group k_step applies
+        int kmax_gpu = 0;        // widest gpu-mode beam (the cluster select is launched from
+                                 // kSelectClusterMinK on)
     };
     std::vector<Group> groups;
     cudaEvent_t fork = nullptr;
@@ -409,6 +411,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     const size_t o_prefix = take(sizeof(int32_t) * (nbeams + 1));
     const size_t o_cprefix = take(sizeof(int32_t) * (nbeams + 1) * kNumChunkSizes);
     const size_t o_kcnt = take(sizeof(int32_t) * off_kcnt);
+    const size_t o_kmm = take(sizeof(uint2) * off_kcnt);
     const size_t o_group = take(sizeof(int32_t) * p->ngroups);
     const size_t o_group_init = take(sizeof(int32_t) * p->ngroups);
     const size_t o_ops = take(sizeof(uint32_t) * ops.size());
@@ -456,6 +459,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
     a.rank_lo = 0;
     a.rank_hi = p->total_ranks;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
+    a.kmm = reinterpret_cast<uint2*>(base + o_kmm);
     a.sb_max = sb_max;
     a.max_n = max_n;
     a.beam_pool = base + o_beam;
@@ -536,7 +540,12 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
                 gr.maxN = std::max(gr.maxN, d.N);
                 gr.nq_mask |= 1 << d.nq;
                 if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
-                if (d.mode <= BSJ_MODE_CLEAN) gr.has_gpu = true; else gr.has_compat = true;
+                if (d.mode <= BSJ_MODE_CLEAN) {
+                    gr.has_gpu = true;
+                    gr.kmax_gpu = std::max(gr.kmax_gpu, d.K);
+                } else {
+                    gr.has_compat = true;
+                }
                 if (d.mode != BSJ_MODE_V2 && d.mode != BSJ_MODE_CLEAN) gr.group_ok = false;
             }
             // k_step: one CTA per chunk
@@ -584,6 +593,11 @@ StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
     a.chunk = kStepVariantChunk[v];
     a.group_step = (gr && gr->group_ok) ? kStepVariantGroup[v] : 0;
     a.select_force = p->select_force;
+    {
+        const int fz = p->select_force;
+        const bool cl = (fz & kSelForceCluster) || (gr && gr->kmax_gpu >= kSelectClusterMinK);
+        a.select_cluster = (cl && !(fz & kSelNoCluster)) ? kSelectCluster : 1;
+    }
     a.chunk_prefix = p->d_cprefix + (size_t)ci * (p->nseg + 1);
     a.chunk_lo = p->cprefix[ci][lo];
     a.chunk_hi = p->cprefix[ci][hi];
@@ -1047,16 +1061,18 @@ bsj_status bsj_plan_set_chunk(bsj_plan* p, int32_t chunk)
 static_assert(BSJ_SELECT_FORCE_LARGE == kSelForceLarge && BSJ_SELECT_NO_LARGE == kSelNoLarge &&
               BSJ_SELECT_NO_DIRECT == kSelNoDirect && BSJ_SELECT_RADIX == kSelForceRadix &&
               BSJ_SELECT_NO_DENSE == kSelNoDense && BSJ_SELECT_RANK_LSD == kSelRankLsd &&
-              BSJ_SELECT_BITONIC == kSelBitonic, "route flags of bsj.h and the kernels differ");
+              BSJ_SELECT_BITONIC == kSelBitonic && BSJ_SELECT_NO_CLUSTER == kSelNoCluster &&
+              BSJ_SELECT_FORCE_CLUSTER == kSelForceCluster, "route flags of bsj.h and the kernels differ");
 static_assert(BSJ_ROUTE_LARGE == kPathLarge && BSJ_ROUTE_DIRECT == kPathDirect && BSJ_ROUTE_BUCKET == kPathBucket &&
               BSJ_ROUTE_RADIX == kPathRadix && BSJ_ROUTE_DENSE == kPathDense &&
               BSJ_ROUTE_RANK_LSD == kPathRankLsd && BSJ_ROUTE_RAW_LSD == kPathRawLsd &&
-              BSJ_ROUTE_BITONIC == kPathBitonic, "route bits of bsj.h and the kernels differ");
+              BSJ_ROUTE_BITONIC == kPathBitonic && BSJ_ROUTE_CLUSTER == kPathCluster, "route bits of bsj.h and the kernels differ");
 
 bsj_status bsj_plan_set_select_route(bsj_plan* p, int32_t flags)
 {
     if (!p) return BSJ_ERR_INVALID;
-    if ((flags & ~kSelAll) != 0 || ((flags & kSelForceLarge) && (flags & kSelNoLarge)))
+    if ((flags & ~kSelAll) != 0 || ((flags & kSelForceLarge) && (flags & kSelNoLarge)) ||
+        ((flags & kSelForceCluster) && (flags & kSelNoCluster)))
         return fail(p->ctx, BSJ_ERR_INVALID, "unknown or contradictory select route flags");
     if (flags == p->select_force) return BSJ_OK;
     // the flags are a launch argument baked into the captured graphs: capture again

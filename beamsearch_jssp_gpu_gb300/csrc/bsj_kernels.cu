@@ -49,6 +49,21 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// A warp's min / max score bits into the chunk's range (s_mm[0] min, s_mm[1] max): the
+// selection takes the level's score range from these instead of a pass over its keys.
+__device__ __forceinline__ void chunk_range_add(uint32_t mn, uint32_t mx, uint32_t* s_mm, int lane)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+        mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    }
+    if (lane == 0 && mn <= mx) {
+        atomicMin(&s_mm[0], mn);
+        atomicMax(&s_mm[1], mx);
+    }
+}
+
 // Programmatic dependent launch.  The level kernels are launched with programmatic stream
 // serialization and wait (griddepcontrol.wait) for their predecessor's completion and
 // memory before touching anything it wrote.  k_step also lets its successor -- the next
@@ -388,6 +403,7 @@ k_step(StepArgs a, int s)
     // (more candidates per CTA) copy it into shared memory once
     __shared__ float s_noise_tab[CH >= 32 ? 1000 : 1];
     __shared__ int s_nv[CH], s_pre[CH], s_kcnt, s_P;
+    __shared__ uint32_t s_mm[2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint8_t* wbuf = smem + (size_t)warp * (kRanksPerWarp + 1) * a.sb_max;
     uint8_t* cb = wbuf + (size_t)kRanksPerWarp * a.sb_max;
@@ -504,16 +520,27 @@ k_step(StepArgs a, int s)
                 }
                 if (lane < CH) s_pre[lane] = x - v;
                 if (lane == 31) s_kcnt = x;
+                if (lane == 0) { s_mm[0] = 0xFFFFFFFFu; s_mm[1] = 0u; }
             }
             __syncthreads();
+            uint32_t mn = 0xFFFFFFFFu, mx = 0u;
             for (int rl = warp; rl < CH; rl += kWarpsPerStepCta) {
                 const int cntk = s_nv[rl];
                 const int dst0 = s_pre[rl];
-                for (int i = lane; i < cntk; i += 32) kdst[dst0 + i] = kstage[(size_t)rl * nst + i];
+                for (int i = lane; i < cntk; i += 32) {
+                    const unsigned long long k = kstage[(size_t)rl * nst + i];
+                    kdst[dst0 + i] = k;
+                    mn = min(mn, (uint32_t)(k >> 32));
+                    mx = max(mx, (uint32_t)(k >> 32));
+                }
             }
-            if (threadIdx.x == 0) a.kcnt[d.kcnt_off + q] = s_kcnt;
+            chunk_range_add(mn, mx, s_mm, lane);
         }
         __syncthreads();
+        if (!compat && threadIdx.x == 0) {
+            a.kcnt[d.kcnt_off + q] = s_kcnt;
+            a.kmm[d.kcnt_off + q] = make_uint2(s_mm[0], s_mm[1]);
+        }
     }
 }
 
@@ -642,6 +669,7 @@ __global__ void __launch_bounds__(kGStepWarps * 32) k_step_g(StepArgs a, int s)
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ __align__(8) unsigned long long s_mbar[kGStepWarps];
     __shared__ int s_nv[CH], s_pre[CH], s_kcnt, s_abort;
+    __shared__ uint32_t s_mm[2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int grp = lane / G, gl = lane % G, gsh = grp * G;
     const int slot = warp * SPW + grp;
@@ -893,17 +921,28 @@ __global__ void __launch_bounds__(kGStepWarps * 32) k_step_g(StepArgs a, int s)
             }
             if (lane < CH) s_pre[lane] = x - v;
             if (lane == 31) s_kcnt = x;
+            if (lane == 0) { s_mm[0] = 0xFFFFFFFFu; s_mm[1] = 0u; }
         }
         __syncthreads();
         unsigned long long* kdst = a.keys + d.key_off + (int64_t)q * CH * n;
+        uint32_t mn = 0xFFFFFFFFu, mx = 0u;
         for (int rl = warp; rl < CH; rl += kGStepWarps) {
             const int cntk = s_nv[rl], dst0 = s_pre[rl];
             const unsigned long long* ks =
                 reinterpret_cast<const unsigned long long*>(smem + (size_t)CH * a.sb_max) + (size_t)rl * a.max_n;
-            for (int x = lane; x < cntk; x += 32) kdst[dst0 + x] = ks[x];
+            for (int x = lane; x < cntk; x += 32) {
+                const unsigned long long k = ks[x];
+                kdst[dst0 + x] = k;
+                mn = min(mn, (uint32_t)(k >> 32));
+                mx = max(mx, (uint32_t)(k >> 32));
+            }
         }
-        if (threadIdx.x == 0) a.kcnt[d.kcnt_off + q] = s_kcnt;
+        chunk_range_add(mn, mx, s_mm, lane);
         __syncthreads();
+        if (threadIdx.x == 0) {
+            a.kcnt[d.kcnt_off + q] = s_kcnt;
+            a.kmm[d.kcnt_off + q] = make_uint2(s_mm[0], s_mm[1]);
+        }
         if (s_abort) break;
     }
 }
@@ -926,14 +965,17 @@ struct SelSmem {
     int* misc;                 // [64]
     unsigned long long* A;     // [kLsdMax]   compacted survivors / radix-sort buffer
     unsigned long long* stg;   // [kStageKeys] staged candidate keys / radix-sort buffer / wide bitonic
+    uint32_t rmin, rmax;       // min / max score bits of the level's keys (from k_step's chunk ranges)
 };
 
 constexpr int kLsdMax = 8192;      // largest survivor count for the radix sort
 constexpr int kStageKeys = 16384;  // candidate keys staged in shared memory
 
-__device__ __forceinline__ SelSmem sel_smem(uint8_t* base)
+__device__ __forceinline__ SelSmem sel_smem(uint8_t* base, uint32_t rmin = 0xFFFFFFFFu, uint32_t rmax = 0u)
 {
     SelSmem s;
+    s.rmin = rmin;
+    s.rmax = rmax;
     s.hist = reinterpret_cast<uint32_t*>(base);
     s.tot = s.hist + 4096;
     s.red = reinterpret_cast<unsigned long long*>(s.tot + 256);
@@ -1067,7 +1109,16 @@ __device__ void stage_keys(const KeySrc& ks, unsigned long long* stg)
     __syncthreads();
 }
 
-// 2a. bucket threshold: returns the number of keys in buckets <= T; misc[2] = T,
+// Bucket of a score (bits) in [smin, smin + 4096 << shift); clamped, so a score outside the
+// recorded range cannot index past the counts.
+__device__ __forceinline__ uint32_t bucket_of(uint32_t sb, uint32_t smin, int shift)
+{
+    const uint32_t b = (sb - smin) >> shift;
+    return b < (uint32_t)kNB ? b : (uint32_t)(kNB - 1);
+}
+
+// 2a. bucket threshold over 4096 linear buckets of the score bits between the level's
+// min and max (S.rmin / S.rmax): returns the number of keys in buckets <= T; misc[2] = T,
 // misc[4] = shift, misc[1] = smin.
 // `each(fn)` calls fn on every key this thread is responsible for.
 template <typename ForEach>
@@ -1077,25 +1128,14 @@ __device__ int bucket_threshold_each(ForEach each, int R, const SelSmem& S)
     uint32_t* cnt = S.hist;
     int* misc = S.misc;
     int* wsum = reinterpret_cast<int*>(S.red);
-    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
-    each([&](unsigned long long k) { const uint32_t sb = (uint32_t)(k >> 32); mn = min(mn, sb); mx = max(mx, sb); });
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
-        mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
-    }
+    (void)lane;
     for (int b = tid; b < kNB; b += nthr) cnt[b] = 0;
-    if (tid == 0) { misc[0] = 0; misc[1] = (int)0xFFFFFFFFu; }
+    if (tid == 0) misc[1] = (int)S.rmin;
     __syncthreads();
-    if (lane == 0) {
-        atomicMax(reinterpret_cast<unsigned*>(&misc[0]), mx);
-        atomicMin(reinterpret_cast<unsigned*>(&misc[1]), mn);
-    }
-    __syncthreads();
-    const uint32_t smin = (uint32_t)misc[1], range = (uint32_t)misc[0] - smin;
+    const uint32_t smin = S.rmin, range = S.rmax - S.rmin;
     const int nbits = range ? 32 - __clz(range) : 0;
     const int shift = nbits > 12 ? nbits - 12 : 0;
-    each([&](unsigned long long k) { atomicAdd(&cnt[(((uint32_t)(k >> 32)) - smin) >> shift], 1u); });
+    each([&](unsigned long long k) { atomicAdd(&cnt[bucket_of((uint32_t)(k >> 32), smin, shift)], 1u); });
     __syncthreads();
     constexpr int BPT = kNB / kSelectThreads;
     uint32_t c4[BPT];
@@ -1970,8 +2010,25 @@ __device__ bool select_direct(unsigned long long* stg, int V, int R, int T, int 
     return true;
 }
 
+// lsd_sort_emit for any count <= kLsdMax (E = ceil(count / kSelectThreads) elements per thread)
+__device__ void lsd_sort_emit_n(unsigned long long* A, unsigned long long* B, int count, int R, uint32_t* sel,
+                                const SelSmem& S)
+{
+    switch ((count + kSelectThreads - 1) / kSelectThreads) {
+    case 0:
+    case 1: lsd_sort_emit<1>(A, B, count, R, sel, S); break;
+    case 2: lsd_sort_emit<2>(A, B, count, R, sel, S); break;
+    case 3: lsd_sort_emit<3>(A, B, count, R, sel, S); break;
+    case 4: lsd_sort_emit<4>(A, B, count, R, sel, S); break;
+    case 5: lsd_sort_emit<5>(A, B, count, R, sel, S); break;
+    case 6: lsd_sort_emit<6>(A, B, count, R, sel, S); break;
+    case 7: lsd_sort_emit<7>(A, B, count, R, sel, S); break;
+    default: lsd_sort_emit<8>(A, B, count, R, sel, S); break;
+    }
+}
+
 __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int V, const KeySrc& ks,
-                           uint8_t* smem)
+                           uint8_t* smem, uint32_t rmin, uint32_t rmax)
 {
     const int tid = threadIdx.x;
     const int P = st.P, K = d.K;
@@ -1979,7 +2036,7 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
     const int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
     const int R = V < keff ? V : keff;
     uint32_t* sel = a.sel + d.sel_off;
-    const SelSmem S = sel_smem(smem);
+    const SelSmem S = sel_smem(smem, rmin, rmax);
     const int fz = a.select_force;    // route flags (0 = by level size); uniform over the block
     // routes taken, recorded by thread 0 with a reduction that returns nothing
     auto route = [&](uint32_t bit) { if (tid == 0) atomicOr(&st.select_paths, bit); };
@@ -2028,7 +2085,6 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
             }
             const int RR = R < count ? R : count;
             if (count <= kLsdMax && !(fz & kSelBitonic)) {
-                const int E = (count + kSelectThreads - 1) / kSelectThreads;
                 int nd = -1;
                 DenseTables D;
                 if (bucketed && !(fz & kSelNoDense)) {
@@ -2057,18 +2113,7 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
                     } else {
                         route(kPathRawLsd);
                     }
-                    unsigned long long* B = S.stg;
-                    switch (E) {
-                    case 0:
-                    case 1: lsd_sort_emit<1>(dst, B, count, RR, sel, S); break;
-                    case 2: lsd_sort_emit<2>(dst, B, count, RR, sel, S); break;
-                    case 3: lsd_sort_emit<3>(dst, B, count, RR, sel, S); break;
-                    case 4: lsd_sort_emit<4>(dst, B, count, RR, sel, S); break;
-                    case 5: lsd_sort_emit<5>(dst, B, count, RR, sel, S); break;
-                    case 6: lsd_sort_emit<6>(dst, B, count, RR, sel, S); break;
-                    case 7: lsd_sort_emit<7>(dst, B, count, RR, sel, S); break;
-                    default: lsd_sort_emit<8>(dst, B, count, RR, sel, S); break;
-                    }
+                    lsd_sort_emit_n(dst, S.stg, count, RR, sel, S);
                 }
             } else {
                 route(kPathBitonic);
@@ -2090,29 +2135,63 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
     }
 }
 
-__global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, int sort_cap)
+// Candidate counts of the level's chunks -> their prefix in s_cpref (nch + 1 entries, up to
+// 2 chunks per thread); returns V, the level's candidate keys, and in rmin / rmax the min
+// and max score bits over the chunks' ranges.  One block scan carries the sum and both
+// reductions; s_red: 100 words of scratch.  Ends synchronised.
+__device__ int level_key_prefix(const StepArgs& a, const SegDesc& d, int nch, int* s_cpref, uint32_t* s_red,
+                                uint32_t& rmin, uint32_t& rmax)
 {
-    extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ int s_cpref[kMaxChunks + 1];
-    __shared__ int s_wsum[72];
-    (void)sort_cap;
-    pdl_wait();
-    const int seg = a.seg_lo + blockIdx.x;
-    const SegDesc& d = a.segs[seg];
-    if (d.mode > MODE_CLEAN || s >= d.N) return;
-    SegState& st = a.st[seg];
-    // candidate counts of the level's chunks -> prefix, V (up to 2 chunks per thread)
     constexpr int CPT = (kMaxChunks + kSelectThreads - 1) / kSelectThreads;
-    const int nch = (d.K + a.chunk - 1) / a.chunk;
-    const int c0 = threadIdx.x * CPT;
+    const int c0 = threadIdx.x * CPT, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    uint32_t* wsum = s_red;        // [32] warp sums, then their exclusive prefixes
+    uint32_t* wmin = s_red + 32;   // [32]
+    uint32_t* wmax = s_red + 64;   // [32]
+    uint32_t* res = s_red + 96;    // [3] total, min, max
     int cv[CPT], v = 0;
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
 #pragma unroll
     for (int u = 0; u < CPT; u++) {
-        cv[u] = (c0 + u < nch) ? a.kcnt[d.kcnt_off + c0 + u] : 0;
+        cv[u] = 0;
+        if (c0 + u < nch) {
+            cv[u] = a.kcnt[d.kcnt_off + c0 + u];
+            const uint2 r = a.kmm[d.kcnt_off + c0 + u];
+            mn = min(mn, r.x);
+            mx = max(mx, r.y);
+        }
         v += cv[u];
     }
-    int V;
-    int pre = block_exclusive_scan(v, &V, s_wsum);
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, x, o);
+        if (lane >= o) x += y;
+        mn = min(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+        mx = max(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    }
+    if (lane == 31) wsum[warp] = (uint32_t)x;
+    if (lane == 0) { wmin[warp] = mn; wmax[warp] = mx; }
+    __syncthreads();
+    if (warp == 0) {
+        const int w = lane < nwarps ? (int)wsum[lane] : 0;
+        uint32_t m0 = lane < nwarps ? wmin[lane] : 0xFFFFFFFFu, m1 = lane < nwarps ? wmax[lane] : 0u;
+        int ws = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, ws, o);
+            if (lane >= o) ws += y;
+            m0 = min(m0, __shfl_xor_sync(FULL_MASK, m0, o));
+            m1 = max(m1, __shfl_xor_sync(FULL_MASK, m1, o));
+        }
+        wsum[lane] = (uint32_t)(ws - w);
+        if (lane == 31) { res[0] = (uint32_t)ws; res[1] = m0; res[2] = m1; }
+    }
+    __syncthreads();
+    int pre = (int)wsum[warp] + x - v;
+    const int V = (int)res[0];
+    rmin = res[1];
+    rmax = res[2];
 #pragma unroll
     for (int u = 0; u < CPT; u++) {
         if (c0 + u < nch) s_cpref[c0 + u] = pre;
@@ -2120,18 +2199,388 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     }
     if (threadIdx.x == 0) s_cpref[nch] = V;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        st.expanded += V;
-        st.slots += (long long)st.P * d.n;
-        if (st.P > 0) st.levels += 1;
-    }
+    return V;
+}
+
+__device__ __forceinline__ void count_level(const SegDesc& d, SegState& st, int V)
+{
+    st.expanded += V;
+    st.slots += (long long)st.P * d.n;
+    if (st.P > 0) st.levels += 1;
+}
+
+__global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, int sort_cap)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_cpref[kMaxChunks + 1];
+    __shared__ uint32_t s_red[100];
+    (void)sort_cap;
+    pdl_wait();
+    const int seg = a.seg_lo + blockIdx.x;
+    const SegDesc& d = a.segs[seg];
+    if (d.mode > MODE_CLEAN || s >= d.N) return;
+    SegState& st = a.st[seg];
+    const int nch = (d.K + a.chunk - 1) / a.chunk;
+    uint32_t rmin, rmax;
+    const int V = level_key_prefix(a, d, nch, s_cpref, s_red, rmin, rmax);
+    if (threadIdx.x == 0) count_level(d, st, V);
     if (s == d.N - 1) return;  // the last level's sort and gather are not observable
     KeySrc ks;
     ks.base = a.keys + d.key_off;
     ks.cpref = s_cpref;
     ks.nch = nch;
     ks.cap = a.chunk * d.n;
-    select_gpu(d, st, a, V, ks, smem);
+    select_gpu(d, st, a, V, ks, smem, rmin, rmax);
+}
+
+// ---- cluster select: one beam's level on the C CTAs of a thread-block cluster ---------
+// The bucket + dense-rank route of select_gpu with its data-parallel phases split: CTA r
+// stages keys [r*V/C, (r+1)*V/C) of the level (slot order), builds its share of every
+// histogram and table, and the CTAs exchange only small summaries through distributed
+// shared memory (ld.shared::cluster of a peer's copy); the level's score range, and with it
+// the bucket mapping, comes from the chunk ranges k_step records:
+//   #1 the 4 096 bucket counts -> the same threshold bucket T in every CTA;
+//   #2 the distinct-score bitmap (each CTA ORs the peers' words into its own; OR is
+//      idempotent, so a peer reading a word before or after the merge sees the same
+//      union) -> identical dense-rank tables;
+//   #3 the per-digit survivor totals -> each survivor's global position
+//      (digits below it in every CTA, its digit in lower CTAs, then its CTA's order).
+// Every CTA scatters its survivors straight into the beam's survivor list.  With more
+// distinct scores than kClusterMaxDigits, or a bitmap larger than kDenseWords, CTA 0
+// gathers the survivors (its own, then the peers', which is slot order) and sorts them by
+// LSD passes over the dense ranks or the raw score bits.  A level with more than kLsdMax
+// survivors is left by all CTAs together after a cluster barrier and CTA 0 runs
+// select_gpu on it; levels of at most kClusterMinKeys keys and forced one-CTA routes run
+// there too.  A CTA only
+// reads a peer's shared memory between two cluster barriers the peer also passes, and the
+// last barrier before exit is split (arrive after the last remote read, wait before exit).
+constexpr int kClusterMaxDigits = 1024;          // dense ranks of one counting pass (10 bits)
+constexpr int kClusterTotOff = kDenseBmOff + kDenseWords;   // (in keys, after bitmap + prefix) i32 digit totals
+constexpr int kClusterBaseOff = kClusterTotOff + kClusterMaxDigits / 2;   // i32[1024] digit bases
+static_assert(32 * kClusterMaxDigits * 2 <= kDenseOccOff * 8, "per-warp digit counters must fit below the tables");
+static_assert(kClusterBaseOff + kClusterMaxDigits / 2 <= kStageKeys, "cluster tables exceed the staging area");
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// all threads of all CTAs of the cluster (release / acquire at cluster scope)
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_sync() { cluster_arrive(); cluster_wait(); }
+// the shared-memory address of `p`'s counterpart in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t peer_addr(const void* p, unsigned rank)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ uint32_t ld_peer(const void* p, unsigned rank)
+{
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(peer_addr(p, rank)) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint4 ld_peer4(const void* p, unsigned rank)
+{
+    uint4 v;
+    asm volatile("ld.shared::cluster.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(peer_addr(p, rank))
+                 : "memory");
+    return v;
+}
+
+// The gathered survivors A[0..count) (slot order) sorted by LSD passes over their dense
+// ranks (D given) or score bits, the first R slots written to sel.  A separate function:
+// its sort instantiations would otherwise spill the cluster route's registers.
+__device__ __noinline__ void gathered_sort(unsigned long long* A, int count, int R, bool ranked, DenseTables D,
+                                          uint32_t* sel, uint8_t* smem)
+{
+    const SelSmem S = sel_smem(smem);
+    if (ranked) {
+        for (int i = threadIdx.x; i < count; i += blockDim.x) {
+            const unsigned long long k = A[i];
+            A[i] = ((unsigned long long)D.rank_of((uint32_t)(k >> 32)) << 32) | (k & 0xFFFFFFFFull);
+        }
+        __syncthreads();
+    }
+    lsd_sort_emit_n(A, S.stg, count, R, sel, S);
+}
+
+// Returns the kPath* bits of the route when the level was selected (survivors 0..R-1
+// written), 0 -- the same in every CTA, after a cluster barrier, nothing written -- when
+// CTA 0 must run select_gpu.  On nonzero the caller still owes the closing cluster_wait().
+template <int C>
+__device__ uint32_t select_cluster(const KeySrc& ks, int V, int R, uint32_t* sel, const SelSmem& S, unsigned rank)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    int* wsum = reinterpret_cast<int*>(S.red);
+    const int lo = (int)((long long)V * rank / C), hi = (int)((long long)V * (rank + 1) / C);
+    const int nl = hi - lo;   // <= kStageKeys: V <= C * kStageKeys
+    unsigned long long* stg = S.stg;
+    // 1. this CTA's keys, slot order, into stg (warp per chunk)
+    for (int c = warp; c < ks.nch; c += nwarps) {
+        const int c0 = ks.cpref[c];
+        const int a0 = max(c0, lo), a1 = min(ks.cpref[c + 1], hi);
+        const unsigned long long* src = ks.base + (size_t)c * ks.cap;
+        for (int i = a0 + lane; i < a1; i += 32) cp_async8(stg + (i - lo), src + (i - c0));
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // 2. bucket counts over the level's score range (from k_step's chunk ranges)
+    uint32_t* cnt = S.hist;
+    int* misc = S.misc;
+    for (int b = tid; b < kNB; b += nthr) cnt[b] = 0;
+    __syncthreads();
+    const uint32_t smin = S.rmin, range = S.rmax - S.rmin;
+    const int nbits = range ? 32 - __clz(range) : 0;
+    const int shift = nbits > 12 ? nbits - 12 : 0;
+    for (int i = tid; i < nl; i += nthr) atomicAdd(&cnt[bucket_of((uint32_t)(stg[i] >> 32), smin, shift)], 1u);
+    cluster_sync();   // #1: every CTA's bucket counts (cnt, read by peers until #2)
+    constexpr int BPT = kNB / kSelectThreads;
+    static_assert(BPT == 4, "one 16-byte peer load per thread");
+    uint32_t g4[BPT];
+    {
+        const uint4 own = *reinterpret_cast<const uint4*>(&cnt[tid * BPT]);
+        g4[0] = own.x; g4[1] = own.y; g4[2] = own.z; g4[3] = own.w;
+#pragma unroll
+        for (int q = 0; q < C; q++) {
+            if (q == (int)rank) continue;
+            const uint4 v = ld_peer4(&cnt[tid * BPT], q);
+            g4[0] += v.x; g4[1] += v.y; g4[2] += v.z; g4[3] += v.w;
+        }
+    }
+    int sum = 0;
+#pragma unroll
+    for (int u = 0; u < BPT; u++) sum += (int)g4[u];
+    int tot;
+    int base = block_exclusive_scan(sum, &tot, wsum);
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        if (base < R && R <= base + (int)g4[u]) { misc[2] = tid * BPT + u; misc[3] = base + (int)g4[u]; }
+        base += (int)g4[u];
+    }
+    __syncthreads();
+    const int T = misc[2], count = misc[3];   // survivors: the keys of buckets <= T, cluster-wide
+    if (count > kLsdMax) { cluster_sync(); return 0u; }
+    // 3. this CTA's survivors, stably compacted into A
+    const uint32_t lim = ((uint32_t)T + 1u) << shift;
+    auto keep = [=](unsigned long long k) { return (((uint32_t)(k >> 32)) - smin) < lim; };
+    auto get_s = [=](int i) { return stg[i]; };
+    unsigned long long* A = S.A;
+    const int cl = compact_stable(get_s, nl, keep, A, kLsdMax, S);
+    // 4. dense-rank tables (stg is free now): occupied-bucket index from the cluster's
+    // counts, this CTA's bits, then the union of the CTAs' bitmaps
+    DenseTables D;
+    D.occ = reinterpret_cast<uint16_t*>(stg + kDenseOccOff);
+    D.bm = reinterpret_cast<uint32_t*>(stg + kDenseBmOff);
+    D.wp = D.bm + kDenseWords;
+    D.W = shift > 5 ? 1 << (shift - 5) : 1;
+    D.shift = shift;
+    D.smin = smin;
+    D.omask = (1u << shift) - 1u;
+    int f[BPT], fs = 0;
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        f[u] = (tid * BPT + u <= T && g4[u] != 0u) ? 1 : 0;
+        fs += f[u];
+    }
+    int O;
+    int ob = block_exclusive_scan(fs, &O, wsum);
+#pragma unroll
+    for (int u = 0; u < BPT; u++) {
+        D.occ[tid * BPT + u] = (uint16_t)ob;
+        ob += f[u];
+    }
+    const int nw = O * D.W;   // the same in every CTA
+    int nd = -1;
+    if (nw <= kDenseWords) {
+        for (int w = tid; w < nw; w += nthr) D.bm[w] = 0u;
+        __syncthreads();
+        for (int i = tid; i < cl; i += nthr) {
+            uint32_t bit;
+            const int w = D.word_of((uint32_t)(A[i] >> 32), bit);
+            atomicOr(&D.bm[w], 1u << bit);
+        }
+        cluster_sync();   // #2: every CTA's bitmap (read by peers until #3); cnt is free again
+        const int per = (nw + nthr - 1) / nthr;
+        int pc = 0;
+        for (int k = 0; k < per; k++) {
+            const int w = tid * per + k;
+            if (w < nw) {
+                uint32_t v = D.bm[w];
+#pragma unroll
+                for (int q = 0; q < C; q++)
+                    if (q != (int)rank) v |= ld_peer(&D.bm[w], q);
+                D.bm[w] = v;
+                pc += __popc(v);
+            }
+        }
+        int pre = block_exclusive_scan(pc, &nd, wsum);
+        for (int k = 0; k < per; k++) {
+            const int w = tid * per + k;
+            if (w < nw) {
+                D.wp[w] = (uint32_t)pre;
+                pre += __popc(D.bm[w]);
+            }
+        }
+    }
+    if (nd < 0 || nd > kClusterMaxDigits) {   // the same in every CTA
+        // too many distinct scores for one counting pass (or no tables): CTA 0 gathers the
+        // survivors -- its own, then each peer's, which is slot order -- and sorts them with
+        // LSD passes (over the dense ranks when the tables exist, else the score bits)
+        if (tid == 0) misc[5] = cl;
+        cluster_sync();   // every CTA's survivors and count (misc[5]); bitmap merges done
+        if (rank == 0) {
+            int off = cl;
+            for (int q = 1; q < C; q++) {
+                const int cq = (int)ld_peer(&misc[5], q);
+                for (int i = tid; i < cq; i += nthr) {
+                    const uint32_t* pk = reinterpret_cast<const uint32_t*>(&A[i]);
+                    const uint32_t lo32 = ld_peer(pk, q), hi32 = ld_peer(pk + 1, q);
+                    A[off + i] = ((unsigned long long)hi32 << 32) | lo32;
+                }
+                off += cq;
+            }
+        }
+        cluster_arrive();  // CTA 0's remote reads are done
+        if (rank == 0) {
+            __syncthreads();
+            gathered_sort(A, count, R, nd >= 0, D, sel, reinterpret_cast<uint8_t*>(S.hist));
+        }
+        return kPathCluster | (nd >= 0 ? kPathRankLsd : kPathRawLsd);
+    }
+    // 5. one stable counting pass by dense rank: per-warp digit counters (u16 [32][ND] over
+    // the start of stg), ranks found with bit ballots, element order within the warp
+    const int db = nd > 1 ? 32 - __clz(nd - 1) : 1;
+    const int ND = 1 << db;
+    uint16_t* wh = reinterpret_cast<uint16_t*>(stg);
+    int* dtot = reinterpret_cast<int*>(stg + kClusterTotOff);
+    int* dbase = reinterpret_cast<int*>(stg + kClusterBaseOff);
+    for (int i = tid; i < 32 * ND / 2; i += nthr) reinterpret_cast<uint32_t*>(wh)[i] = 0u;
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    const int E = (cl + nthr - 1) / nthr;
+#pragma unroll 1
+    for (int e = 0; e < E; e++) {
+        const int p = warp * 32 * E + e * 32 + lane;
+        const bool valid = p < cl;
+        const unsigned long long x = valid ? A[p] : 0ull;
+        const int d = valid ? (int)D.rank_of((uint32_t)(x >> 32)) : 0;
+        unsigned grp = __ballot_sync(FULL_MASK, valid);
+#pragma unroll 1
+        for (int bit = 0; bit < db; bit++) {
+            const unsigned bb = __ballot_sync(FULL_MASK, (d >> bit) & 1);
+            grp &= ((d >> bit) & 1) ? bb : ~bb;
+        }
+        const int r_in = __popc(grp & lt);
+        int b = 0;
+        if (valid) b = wh[warp * ND + d];
+        __syncwarp();
+        if (valid && r_in == 0) wh[warp * ND + d] = (uint16_t)(b + __popc(grp));
+        __syncwarp();
+        if (valid)
+            A[p] = ((unsigned long long)d << 48) | ((unsigned long long)(b + r_in) << 32) | (x & 0xFFFFFFFFull);
+    }
+    __syncthreads();
+    if (tid < ND) {
+        int run = 0;
+        for (int w = 0; w < nwarps; w++) {
+            const int t = wh[w * ND + tid];
+            wh[w * ND + tid] = (uint16_t)run;
+            run += t;
+        }
+        dtot[tid] = run;
+    }
+    cluster_sync();   // #3: every CTA's digit totals (read by peers until the closing wait)
+    int g = 0, lower = 0;
+    if (tid < ND) {
+#pragma unroll
+        for (int q = 0; q < C; q++) {
+            const int t = q == (int)rank ? dtot[tid] : (int)ld_peer(&dtot[tid], q);
+            g += t;
+            if (q < (int)rank) lower += t;
+        }
+    }
+    cluster_arrive();  // this CTA's remote reads are done
+    int gt;
+    const int gb = block_exclusive_scan(g, &gt, wsum);
+    if (tid < ND) dbase[tid] = gb + lower;
+    __syncthreads();
+#pragma unroll 1
+    for (int e = 0; e < E; e++) {
+        const int p = warp * 32 * E + e * 32 + lane;
+        if (p < cl) {
+            const unsigned long long x = A[p];
+            const int dg = (int)(x >> 48);
+            const int pos = dbase[dg] + (int)wh[warp * ND + dg] + (int)((x >> 32) & 0xFFFFull);
+            if (pos < R) sel[pos] = (uint32_t)(x & 0xFFFFFFFFull);
+        }
+    }
+    return kPathCluster;
+}
+
+// the one-CTA routes as a separate function: the cluster kernel's registers stay for its own route
+__device__ __noinline__ void select_gpu_fallback(const SegDesc& d, SegState& st, const StepArgs& a, int V,
+                                                 const KeySrc& ks, uint8_t* smem, uint32_t rmin, uint32_t rmax)
+{
+    select_gpu(d, st, a, V, ks, smem, rmin, rmax);
+}
+
+// k_select launched as clusters of C CTAs per beam (blocks C*b .. C*b+C-1 serve beam
+// seg_lo + b).  Levels the cluster route takes run on all C CTAs; the rest run select_gpu
+// on CTA 0 while the others leave.
+template <int C>
+__global__ void __launch_bounds__(kSelectThreads) k_select_cl(StepArgs a, int s, int sort_cap)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_cpref[kMaxChunks + 1];
+    __shared__ uint32_t s_red[100];
+    (void)sort_cap;
+    pdl_wait();
+    const unsigned rank = cluster_rank();
+    const int seg = a.seg_lo + (int)(blockIdx.x / C);
+    const SegDesc& d = a.segs[seg];
+    if (d.mode > MODE_CLEAN || s >= d.N) return;   // the same for the whole cluster
+    SegState& st = a.st[seg];
+    const int nch = (d.K + a.chunk - 1) / a.chunk;
+    uint32_t rmin, rmax;
+    const int V = level_key_prefix(a, d, nch, s_cpref, s_red, rmin, rmax);
+    const int P = st.P, K = d.K;
+    if (rank == 0 && threadIdx.x == 0) count_level(d, st, V);
+    if (s == d.N - 1) return;  // the last level's sort and gather are not observable
+    KeySrc ks;
+    ks.base = a.keys + d.key_off;
+    ks.cpref = s_cpref;
+    ks.nch = nch;
+    ks.cap = a.chunk * d.n;
+    const int total = P * d.n;
+    const int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
+    const int R = V < keff ? V : keff;
+    const int fz = a.select_force;
+    const bool take = (fz & ~kSelForceCluster) == 0 && R > 0 && K <= kLsdMax && V <= C * kStageKeys &&
+                      ((fz & kSelForceCluster) || V > kClusterMinKeys);
+    uint32_t* sel = a.sel + d.sel_off;
+    const uint32_t path = take ? select_cluster<C>(ks, V, R, sel, sel_smem(smem, rmin, rmax), rank) : 0u;
+    if (path) {
+        if (rank == 0) {
+            if (threadIdx.x == 0) atomicOr(&st.select_paths, path);
+            __syncthreads();
+            select_fillers(d, a, P, R, keff, sel, smem);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                st.P = keff;
+                st.materialized += keff;
+            }
+        }
+        cluster_wait();   // peers may read this CTA's digit totals until here
+        return;
+    }
+    if (rank == 0) select_gpu_fallback(d, st, a, V, ks, smem, rmin, rmax);
 }
 
 // ------------------------------------------------------------------------------------
@@ -2719,6 +3168,8 @@ static cudaError_t set_carveout()
 {
     const int c = cudaSharedmemCarveoutMaxShared;
     cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_select_cl<kSelectCluster>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
@@ -2749,6 +3200,7 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = set_carveout();
     if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<kSelectCluster>, select_smem_bytes(sort_cap));
     if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
@@ -2761,6 +3213,7 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
 {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<kSelectCluster>, select_smem_bytes(sort_cap));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     if (e == cudaSuccess)
@@ -2835,8 +3288,29 @@ cudaError_t launch_gather_v1(const StepArgs& a, int s, int grid, cudaStream_t st
 
 cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t stream)
 {
-    return launch_kernel(k_select, a.seg_hi - a.seg_lo, kSelectThreads, select_smem_bytes(sort_cap), stream, true,
-                         a, s, sort_cap);
+    const int nseg = a.seg_hi - a.seg_lo;
+    if (a.select_cluster <= 1)
+        return launch_kernel(k_select, nseg, kSelectThreads, select_smem_bytes(sort_cap), stream, true, a, s,
+                             sort_cap);
+    if (a.select_cluster != kSelectCluster) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(nseg * kSelectCluster));
+    cfg.blockDim = dim3((unsigned)kSelectThreads);
+    cfg.dynamicSmemBytes = select_smem_bytes(sort_cap);
+    cfg.stream = stream;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kSelectCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (BSJ_PDL) {
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.numAttrs = 2;
+    }
+    return cudaLaunchKernelEx(&cfg, k_select_cl<kSelectCluster>, a, s, sort_cap);
 }
 
 cudaError_t launch_heap(const StepArgs& a, int s, const HeapCfg& hc, cudaStream_t stream)

@@ -15,6 +15,8 @@ struct StepArgs {
     const int32_t* rank_prefix;   // [nseg+1] prefix sums of K (flattened rank space)
     const int32_t* chunk_prefix;  // [nseg+1] prefix sums of ceil(K/chunk)
     int32_t* kcnt;                // candidate keys per chunk of the current level
+    uint2* kmm;                   // per chunk of the current level: min / max score bits of
+                                  // its keys ({~0, 0} when it has none)
     int32_t nseg;
     int32_t total_ranks;
     int32_t total_chunks;
@@ -29,6 +31,7 @@ struct StepArgs {
     int32_t select_force;         // kSel* route flags for k_select (0 = by level size)
     int32_t group_step;           // k_step form: 0 warp per survivor; 1-4 a lane group per
                                   // survivor (k_step_g: 4 lanes copy / bulk, 8 lanes copy / bulk)
+    int32_t select_cluster;       // CTAs per beam of k_select: 1, or kSelectCluster (cluster launch)
     uint8_t* beam_pool;
     uint8_t* slot_pool;
     unsigned long long* keys;

@@ -160,6 +160,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     const size_t o_prefix = take(2 * sizeof(int32_t));
     const size_t o_cprefix = take(2 * sizeof(int32_t));
     const size_t o_kcnt = take((size_t)nch * sizeof(int32_t));
+    const size_t o_kmm = take((size_t)nch * sizeof(uint2));
     const size_t o_group = take(sizeof(int32_t));
     const size_t o_ops = take(N * sizeof(uint32_t));
     const size_t o_beam = take(2 * align_up(K * d.sbytes, 256));
@@ -204,6 +205,7 @@ extern "C" bsj_status bsj_solve_noalloc(int32_t n, int32_t m, const int32_t* d_m
     a.chunk_prefix = reinterpret_cast<const int32_t*>(base + o_cprefix);
     a.total_chunks = nch;
     a.kcnt = reinterpret_cast<int32_t*>(base + o_kcnt);
+    a.kmm = reinterpret_cast<uint2*>(base + o_kmm);
     a.sb_max = d.sbytes;
     a.max_n = n;
     a.beam_pool = base + o_beam;

@@ -217,7 +217,8 @@ class Plan:
     def set_select_route(self, *flags: str):
         """Force the gpu-mode levels' top-K selection onto routes (names of
         ``_native.SELECT``: force_large, no_large, no_direct, radix, no_dense, rank_lsd,
-        bitonic); no names = the normal choice by level size (bsj_plan_set_select_route)."""
+        bitonic, no_cluster, force_cluster); no names = the normal choice by level size
+        (bsj_plan_set_select_route)."""
         v = 0
         for f in flags:
             v |= nat.SELECT[f]

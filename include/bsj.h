@@ -169,7 +169,16 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches
    give the same stable (score, slot) order.  bsj_plan_set_select_route forces the plan's
    levels onto routes (BSJ_SELECT_* flags OR'd; 0 = the normal choice), so every route
    can be checked on small inputs; the plan's captured graphs are rebuilt on its next
-   run.  BSJ_SELECT_FORCE_LARGE and BSJ_SELECT_NO_LARGE exclude each other.
+   run.  Beam groups whose widest gpu-mode beam has K >= 4096 run the selection as a
+   cluster of 2 thread blocks per beam, which split the level's keys and exchange only
+   summaries through distributed shared memory (route CLUSTER: the bucket + dense-rank
+   route on both blocks) on levels of more than 8192 candidate keys; smaller levels and
+   those it cannot take fall back to the one-block routes.
+   BSJ_SELECT_NO_CLUSTER keeps one block per beam, BSJ_SELECT_FORCE_CLUSTER launches the
+   cluster form whatever K and takes its route on every level it can (any size).
+   BSJ_SELECT_FORCE_LARGE and BSJ_SELECT_NO_LARGE exclude each other, and so do
+   BSJ_SELECT_FORCE_CLUSTER and BSJ_SELECT_NO_CLUSTER; with any other flag set the cluster
+   form runs the one-block routes on its first block.
    bsj_plan_select_routes: BSJ_ROUTE_* bits of the routes the last run took (OR over the
    plan's beams and levels; waits for the run). */
 #define BSJ_SELECT_FORCE_LARGE 1  /* large-level route (keys read in place) at any size */
@@ -179,6 +188,8 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches
 #define BSJ_SELECT_NO_DENSE    16 /* LSD passes over the raw score bits */
 #define BSJ_SELECT_RANK_LSD    32 /* dense ranks written into the keys, then LSD passes */
 #define BSJ_SELECT_BITONIC     64 /* block bitonic sort of the survivors */
+#define BSJ_SELECT_NO_CLUSTER  128 /* one thread block per beam */
+#define BSJ_SELECT_FORCE_CLUSTER 256 /* cluster form and route at any size */
 #define BSJ_ROUTE_LARGE    1
 #define BSJ_ROUTE_DIRECT   2
 #define BSJ_ROUTE_BUCKET   4
@@ -187,6 +198,7 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches
 #define BSJ_ROUTE_RANK_LSD 32
 #define BSJ_ROUTE_RAW_LSD  64
 #define BSJ_ROUTE_BITONIC  128
+#define BSJ_ROUTE_CLUSTER  256
 bsj_status bsj_plan_set_select_route(bsj_plan *plan, int32_t flags);
 bsj_status bsj_plan_select_routes(bsj_plan *plan, uint32_t *routes);
 

@@ -13,6 +13,8 @@ synthetic instance of generator seed 0, all in one plan; the same is done here f
   * the oracle (tests/golden/k4096.json "oracle", from tests/golden/gen_k4096.py): the
     makespan, scored children, slots, levels and the SHA-256 of the schedule, in every
     mode.
+At this K the selection runs as a 2-block cluster per beam; gpu-v2 is also checked with
+the one-block form (the route flags "no_cluster"), so both are pinned at this size.
 The 8 beams share one bound group (one device best-makespan word, updated by atomicMin),
 as in the measured plan; within a pass every beam prunes against the frozen bound
 best_known (500000 here), as the reference does, so the shared word ends as the best of
@@ -46,13 +48,17 @@ def _sha(seq):
     return hashlib.sha256(np.ascontiguousarray(seq, dtype="<i4").tobytes()).hexdigest()
 
 
-def _eight_beams(ctx, n, m, mode):
+def _eight_beams(ctx, n, m, mode, flags=(), routes=None):
     """The measured plan: 8 seeded beams of one instance in one set of launches."""
     mc, du = synthetic_instance(n, m, 0)
     plan = ctx.plan([(mc, du)], [BeamSpec(mode, K, 500000, s, 0, 0) for s in SEEDS])
     try:
+        if flags:
+            plan.set_select_route(*flags)
         plan.run()
         res = plan.results()
+        if routes is not None and mode in ("v1", "v2", "clean"):
+            routes.update(plan.select_routes())
     finally:
         plan.close()
     if mode in ("v1", "v2", "clean"):
@@ -80,10 +86,12 @@ def _check_oracle(got, recs, what):
         assert _sha(g["seq"]) == r["seq_sha256"], w
 
 
-@pytest.mark.parametrize("n,m", [(50, 20), (100, 20)])
-@pytest.mark.parametrize("mode", ["v2", "v1"])
-def test_gpu_modes_match_reference_kernels_and_oracle(ctx, n, m, mode):
-    got = _eight_beams(ctx, n, m, mode)
+@pytest.mark.parametrize("n,m,mode,flags", [(50, 20, "v2", ()), (100, 20, "v2", ()), (50, 20, "v1", ()),
+                                            (100, 20, "v1", ()), (50, 20, "v2", ("no_cluster",))])
+def test_gpu_modes_match_reference_kernels_and_oracle(ctx, n, m, mode, flags):
+    routes = set()
+    got = _eight_beams(ctx, n, m, mode, flags, routes)
+    assert ("cluster" in routes) == (not flags), sorted(routes)
     ref = {r["seed"]: r for r in _load(REF_GPU)["records"]
            if r["mode"] == mode and (r["n"], r["m"]) == (n, m) and r["K"] == K}
     assert sorted(ref) == SEEDS

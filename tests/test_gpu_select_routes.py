@@ -4,7 +4,10 @@ The selection kernel replaces the reference's full stable sort of all child slot
 (cub::DeviceRadixSort::SortPairs, gpu/v1/solver.cu:255-258, gpu/v2_twophases/solver.cu:
 336-339).  By level size it normally takes the direct staged pass or bucket compaction +
 dense-rank sort; the radix-select, raw-LSD, rank-LSD, bitonic and large-level routes run
-only on rare or large levels.  bsj_plan_set_select_route forces them onto small levels,
+only on rare or large levels.  Beams of K >= 4096 run it as a 2-block cluster (the
+bucket + dense-rank route split over both blocks on levels of more than 8 192 keys, the
+one-block routes as its fallback).
+bsj_plan_set_select_route forces them onto small levels,
 and each forced search must equal the oracle bit for bit (makespan, schedule, scored
 children, slots, levels) -- where a wrong tie order would show -- and must report that
 the forced route ran (bsj_plan_select_routes).
@@ -31,6 +34,7 @@ SMALL_ROUTES = [
     (("no_direct", "bitonic"), {"bucket", "bitonic"}),
     (("radix",), {"radix", "raw_lsd"}),
     (("radix", "bitonic"), {"radix", "bitonic"}),
+    (("force_cluster",), {"cluster"}),
 ]
 # levels wider than the shared-memory staging area (more than 16 384 candidate keys)
 LARGE_ROUTES = [
@@ -41,6 +45,8 @@ LARGE_ROUTES = [
     (("no_large", "bitonic"), {"bucket", "bitonic"}),
     (("no_large", "radix"), {"radix", "raw_lsd"}),
     (("no_large", "radix", "bitonic"), {"radix", "bitonic"}),
+    # up to 32 768 keys: staged over the two blocks of the cluster
+    (("force_cluster",), {"cluster"}),
 ]
 
 
@@ -110,14 +116,30 @@ def test_forced_routes_large_levels(ctx, mode):
 @pytest.mark.parametrize("mode", ["v2", "clean"])
 def test_forced_routes_wide_beam(ctx, mode):
     """K=16384 (more survivors than the 8 192-key radix buffer): normally the large-level
-    route; with it excluded, the MSD radix select and the 16 384-key bitonic sort."""
+    route; with it excluded, the MSD radix select and the 16 384-key bitonic sort; in the
+    cluster form (launched by default at this K), the one-block routes on its first block."""
     mc, du = synthetic_instance(16, 3, 3)
     want = O.solve(mc, du, mode, 16384, 0)
-    for flags, must in (((), {"large"}), (("no_large",), {"radix", "bitonic"})):
+    for flags, must in (((), {"large"}), (("no_large",), {"radix", "bitonic"}),
+                        (("no_cluster",), {"large"})):
         got, routes = _run(ctx, mc, du, mode, 16384, 0, flags)
         what = (mode, flags, sorted(routes))
         _same(got, want, what)
         assert must <= routes, what
+
+
+@pytest.mark.parametrize("mode", ["v2", "v1"])
+def test_cluster_route_default_and_off(ctx, mode):
+    """K=4096 on 20x15 (levels of up to ~15 000 keys): the cluster route by default (levels
+    of at most 8 192 keys take the one-block routes on its first block), the one-block
+    bucket route with the cluster form off; both equal the oracle."""
+    mc, du = synthetic_instance(20, 15, 1)
+    want = O.solve(mc, du, mode, 4096, 5)
+    for flags, must, never in (((), {"cluster"}, set()), (("no_cluster",), {"bucket"}, {"cluster"})):
+        got, routes = _run(ctx, mc, du, mode, 4096, 5, flags)
+        what = (mode, flags, sorted(routes))
+        _same(got, want, what)
+        assert must <= routes and not (never & routes), what
 
 
 def test_route_flags_rejected(ctx):
@@ -126,8 +148,11 @@ def test_route_flags_rejected(ctx):
     try:
         with pytest.raises(Exception):
             plan.set_select_route("force_large", "no_large")
+        with pytest.raises(Exception):
+            plan.set_select_route("force_cluster", "no_cluster")
         from beamsearch_jssp_gpu_gb300 import _native as nat
 
         assert plan.lib.bsj_plan_set_select_route(plan.h, 1 << 9) == nat.BSJ_ERR_INVALID
+        assert plan.lib.bsj_plan_set_select_route(plan.h, 1 << 10) == nat.BSJ_ERR_INVALID
     finally:
         plan.close()
