@@ -36,6 +36,18 @@ __device__ __forceinline__ int find_seg(const int32_t* prefix, int lo, int hi, i
     return lo;
 }
 
+// The beam descriptor (constant for a plan, written before its first launch) pulled into L1
+// before the selection waits on its producer, so its reads after the wait hit.  (In k_step,
+// whose CTAs are many and short, the same prefetch measured slower.)
+__device__ __forceinline__ void prefetch_desc(const SegDesc* d)
+{
+    const char* p = reinterpret_cast<const char*>(d);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + sizeof(SegDesc) - 1));
+}
+static_assert(sizeof(SegDesc) > 128, "prefetch_desc touches offsets 0, 128 and the last byte");
+
 __device__ __forceinline__ uint32_t op_info(const uint32_t* ops, int op_off, int j, int m, int k)
 {
     return __ldg(ops + op_off + j * m + k);
@@ -2027,11 +2039,11 @@ __device__ void lsd_sort_emit_n(unsigned long long* A, unsigned long long* B, in
     }
 }
 
-__device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int V, const KeySrc& ks,
+__device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, int P, int V, const KeySrc& ks,
                            uint8_t* smem, uint32_t rmin, uint32_t rmax)
 {
     const int tid = threadIdx.x;
-    const int P = st.P, K = d.K;
+    const int K = d.K;
     const int total = P * d.n;
     const int keff = (d.mode == MODE_CLEAN) ? (V < K ? V : K) : (total < K ? total : K);
     const int R = V < keff ? V : keff;
@@ -2131,7 +2143,7 @@ __device__ void select_gpu(const SegDesc& d, SegState& st, const StepArgs& a, in
     __syncthreads();
     if (tid == 0) {
         st.P = keff;
-        st.materialized += keff;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st.materialized), (unsigned long long)keff);
     }
 }
 
@@ -2202,11 +2214,12 @@ __device__ int level_key_prefix(const StepArgs& a, const SegDesc& d, int nch, in
     return V;
 }
 
-__device__ __forceinline__ void count_level(const SegDesc& d, SegState& st, int V)
+// The level's counters, as reductions (no round trip on the selection's path).
+__device__ __forceinline__ void count_level(int n, SegState& st, int P, int V)
 {
-    st.expanded += V;
-    st.slots += (long long)st.P * d.n;
-    if (st.P > 0) st.levels += 1;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&st.expanded), (unsigned long long)V);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&st.slots), (unsigned long long)P * (unsigned long long)n);
+    if (P > 0) atomicAdd(&st.levels, 1);
 }
 
 __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, int sort_cap)
@@ -2215,22 +2228,24 @@ __global__ void __launch_bounds__(kSelectThreads) k_select(StepArgs a, int s, in
     __shared__ int s_cpref[kMaxChunks + 1];
     __shared__ uint32_t s_red[100];
     (void)sort_cap;
-    pdl_wait();
     const int seg = a.seg_lo + blockIdx.x;
     const SegDesc& d = a.segs[seg];
+    if (threadIdx.x == 0) prefetch_desc(&d);
+    pdl_wait();
     if (d.mode > MODE_CLEAN || s >= d.N) return;
     SegState& st = a.st[seg];
+    const int P = st.P;   // issued with the prefix's loads
     const int nch = (d.K + a.chunk - 1) / a.chunk;
     uint32_t rmin, rmax;
     const int V = level_key_prefix(a, d, nch, s_cpref, s_red, rmin, rmax);
-    if (threadIdx.x == 0) count_level(d, st, V);
+    if (threadIdx.x == 0) count_level(d.n, st, P, V);
     if (s == d.N - 1) return;  // the last level's sort and gather are not observable
     KeySrc ks;
     ks.base = a.keys + d.key_off;
     ks.cpref = s_cpref;
     ks.nch = nch;
     ks.cap = a.chunk * d.n;
-    select_gpu(d, st, a, V, ks, smem, rmin, rmax);
+    select_gpu(d, st, a, P, V, ks, smem, rmin, rmax);
 }
 
 // ---- cluster select: one beam's level on the C CTAs of a thread-block cluster ---------
@@ -2525,10 +2540,10 @@ __device__ uint32_t select_cluster(const KeySrc& ks, int V, int R, uint32_t* sel
 }
 
 // the one-CTA routes as a separate function: the cluster kernel's registers stay for its own route
-__device__ __noinline__ void select_gpu_fallback(const SegDesc& d, SegState& st, const StepArgs& a, int V,
+__device__ __noinline__ void select_gpu_fallback(const SegDesc& d, SegState& st, const StepArgs& a, int P, int V,
                                                  const KeySrc& ks, uint8_t* smem, uint32_t rmin, uint32_t rmax)
 {
-    select_gpu(d, st, a, V, ks, smem, rmin, rmax);
+    select_gpu(d, st, a, P, V, ks, smem, rmin, rmax);
 }
 
 // k_select launched as clusters of C CTAs per beam (blocks C*b .. C*b+C-1 serve beam
@@ -2541,17 +2556,19 @@ __global__ void __launch_bounds__(kSelectThreads) k_select_cl(StepArgs a, int s,
     __shared__ int s_cpref[kMaxChunks + 1];
     __shared__ uint32_t s_red[100];
     (void)sort_cap;
-    pdl_wait();
     const unsigned rank = cluster_rank();
     const int seg = a.seg_lo + (int)(blockIdx.x / C);
     const SegDesc& d = a.segs[seg];
+    if (threadIdx.x == 0) prefetch_desc(&d);
+    pdl_wait();
     if (d.mode > MODE_CLEAN || s >= d.N) return;   // the same for the whole cluster
     SegState& st = a.st[seg];
+    const int P = st.P;   // issued with the prefix's loads
     const int nch = (d.K + a.chunk - 1) / a.chunk;
     uint32_t rmin, rmax;
     const int V = level_key_prefix(a, d, nch, s_cpref, s_red, rmin, rmax);
-    const int P = st.P, K = d.K;
-    if (rank == 0 && threadIdx.x == 0) count_level(d, st, V);
+    const int K = d.K;
+    if (rank == 0 && threadIdx.x == 0) count_level(d.n, st, P, V);
     if (s == d.N - 1) return;  // the last level's sort and gather are not observable
     KeySrc ks;
     ks.base = a.keys + d.key_off;
@@ -2574,13 +2591,13 @@ __global__ void __launch_bounds__(kSelectThreads) k_select_cl(StepArgs a, int s,
             __syncthreads();
             if (threadIdx.x == 0) {
                 st.P = keff;
-                st.materialized += keff;
+                atomicAdd(reinterpret_cast<unsigned long long*>(&st.materialized), (unsigned long long)keff);
             }
         }
         cluster_wait();   // peers may read this CTA's digit totals until here
         return;
     }
-    if (rank == 0) select_gpu_fallback(d, st, a, V, ks, smem, rmin, rmax);
+    if (rank == 0) select_gpu_fallback(d, st, a, P, V, ks, smem, rmin, rmax);
 }
 
 // ------------------------------------------------------------------------------------
