@@ -34,7 +34,7 @@ EXPORTED = [
     "bsj_plan_estimate", "bsj_plan_device_bytes", "bsj_plan_update",
     "bsj_server_create", "bsj_server_destroy", "bsj_submit", "bsj_poll", "bsj_wait", "bsj_server_get_stats",
     "bsj_plan_autotune", "bsj_plan_set_chunk", "bsj_plan_chunk", "bsj_set_autotune",
-    "bsj_plan_set_select_route", "bsj_plan_select_routes", "bsj_server_prepare",
+    "bsj_plan_set_select_route", "bsj_plan_select_routes", "bsj_server_prepare", "bsj_plan_set_select_cluster",
 ]
 # top-K selection routes (include/bsj.h BSJ_SELECT_* / BSJ_ROUTE_*)
 SELECT = {"force_large": 1, "no_large": 2, "no_direct": 4, "radix": 8, "no_dense": 16, "rank_lsd": 32,
@@ -47,7 +47,7 @@ CHUNK_CANDIDATES = (0, 8, 16, 32, 1, 2, 3, 4)  # the autotuner's candidates: 0 =
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("max_inflight", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    _fields_ = [("max_inflight", ctypes.c_int32), ("cluster_inflight", ctypes.c_int32),
                 ("memory_budget", ctypes.c_int64)]
 
 
@@ -172,7 +172,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     for name in ("bsj_create", "bsj_solve", "bsj_solve_batch", "bsj_solve_iterations",
                  "bsj_plan_create", "bsj_plan_run", "bsj_plan_results", "bsj_plan_stats",
                  "bsj_plan_set_timing", "bsj_plan_kernel_ms", "bsj_plan_autotune", "bsj_plan_set_chunk",
-                 "bsj_set_autotune", "bsj_plan_set_select_route", "bsj_plan_select_routes"):
+                 "bsj_set_autotune", "bsj_plan_set_select_route", "bsj_plan_select_routes",
+                 "bsj_plan_set_select_cluster"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

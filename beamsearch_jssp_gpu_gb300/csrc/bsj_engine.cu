@@ -98,8 +98,11 @@ struct bsj_plan {
     int32_t* d_group_init = nullptr;
     size_t beam_bytes = 0, slot_bytes = 0;
     StepArgs args{};
-    // graphs per chunk variant: [0] plain, [1] with timing events recorded around each launch
-    cudaGraphExec_t graph[kNumStepVariants + 1][2] = {};
+    // graphs per chunk variant: [0] plain, [1] with timing events recorded around each
+    // launch; [2], [3] the same with the cluster select switched off
+    cudaGraphExec_t graph[kNumStepVariants + 1][4] = {};
+    bool select_cluster = true;   // bsj_plan_set_select_cluster: the cluster select where the rule picks it
+    bool cluster_matters = false; // some beam group is wide enough for the rule to pick it
     // timing
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -556,6 +559,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             }
             const int wr = (p->prefix[hi] - p->prefix[lo] + kWarpsPerStepCta - 1) / kWarpsPerStepCta;
             gr.gather_grid = std::max(1, std::min(wr, ctx->sm_count * 8));
+            if (gr.has_gpu && gr.kmax_gpu >= kSelectClusterMinK) p->cluster_matters = true;
             p->groups.push_back(gr);
             lo = hi;
         }
@@ -595,7 +599,7 @@ StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
     a.select_force = p->select_force;
     {
         const int fz = p->select_force;
-        const bool cl = (fz & kSelForceCluster) || (gr && gr->kmax_gpu >= kSelectClusterMinK);
+        const bool cl = (fz & kSelForceCluster) || (p->select_cluster && gr && gr->kmax_gpu >= kSelectClusterMinK);
         a.select_cluster = (cl && !(fz & kSelNoCluster)) ? kSelectCluster : 1;
     }
     a.chunk_prefix = p->d_cprefix + (size_t)ci * (p->nseg + 1);
@@ -808,6 +812,52 @@ bsj_status solve_batch_impl(bsj_context* ctx, int num_instances, const bsj_insta
 // =====================================================================================
 // C ABI
 // =====================================================================================
+// The plan's graph for its current chunk variant, timing and selection form, captured on
+// first use (on the context's stream; it replays on any stream).
+static bsj_status plan_graph(bsj_plan* p, cudaGraphExec_t** out)
+{
+    bsj_context* ctx = p->ctx;
+    const bool cluster = p->select_cluster || !p->cluster_matters;   // one graph when it cannot differ
+    const int gi = (p->timing ? 1 : 0) + (cluster ? 0 : 2);
+    cudaGraphExec_t& graph = p->graph[p->variant][gi];
+    if (!graph) {
+        cudaStream_t cap = ctx->stream;
+        cudaGraph_t g = nullptr;
+        BSJ_CUDA(ctx, cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_run(p, cap, true);
+        cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ctx, e, "plan capture"); }
+        if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { graph = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+    }
+    *out = &graph;
+    return BSJ_OK;
+}
+
+// Captures the plan's (untimed) graphs of both selection forms without running them, so a
+// server can switch forms per request without a capture on its path.
+namespace bsj {
+bsj_status plan_capture_forms(bsj_plan* p)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    cudaSetDevice(p->ctx->device);
+    const bool keep_cluster = p->select_cluster, keep_timing = p->timing;
+    p->timing = false;
+    bsj_status st = BSJ_OK;
+    for (int on = 1; on >= 0 && st == BSJ_OK; on--) {
+        p->select_cluster = on != 0;
+        cudaGraphExec_t* graph = nullptr;
+        st = plan_graph(p, &graph);
+        if (!p->cluster_matters) break;
+    }
+    p->select_cluster = keep_cluster;
+    p->timing = keep_timing;
+    return st;
+}
+}  // namespace bsj
+
 extern "C" {
 
 const char* bsj_version(void) { return kVersion; }
@@ -908,22 +958,10 @@ bsj_status bsj_plan_run(bsj_plan* p, void* stream)
     cudaSetDevice(ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     p->last_stream = s;
-    const int gi = p->timing ? 1 : 0;
-    cudaGraphExec_t& graph = p->graph[p->variant][gi];
-    if (!graph) {
-        // capture once on the context's stream, replay on any stream
-        cudaStream_t cap = ctx->stream;
-        cudaGraph_t g = nullptr;
-        BSJ_CUDA(ctx, cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_run(p, cap, true);
-        cudaError_t e2 = cudaStreamEndCapture(cap, &g);
-        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(ctx, e, "plan capture"); }
-        if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) { graph = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
-    }
-    BSJ_CUDA(ctx, cudaGraphLaunch(graph, s));
+    cudaGraphExec_t* graph = nullptr;
+    const bsj_status st = plan_graph(p, &graph);
+    if (st != BSJ_OK) return st;
+    BSJ_CUDA(ctx, cudaGraphLaunch(*graph, s));
     return BSJ_OK;
 }
 
@@ -1081,6 +1119,13 @@ bsj_status bsj_plan_set_select_route(bsj_plan* p, int32_t flags)
         for (cudaGraphExec_t& g : gv)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     p->select_force = flags;
+    return BSJ_OK;
+}
+
+bsj_status bsj_plan_set_select_cluster(bsj_plan* p, int32_t enable)
+{
+    if (!p) return BSJ_ERR_INVALID;
+    p->select_cluster = enable != 0;   // each form's graph is captured once and kept
     return BSJ_OK;
 }
 

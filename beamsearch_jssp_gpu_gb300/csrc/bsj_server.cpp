@@ -81,6 +81,7 @@ struct bsj_server {
     bsj_context* est_ctx = nullptr;  // bsj_submit's footprint checks (under mu)
     int device = 0;
     int64_t budget = 0;
+    int cluster_inflight = 0;   // others in flight up to which a request runs the cluster select
     std::vector<Slot> slots;
 
     std::mutex mu;
@@ -100,7 +101,7 @@ struct bsj_server {
     std::thread worker;
 
     void run();
-    bool admit_one(Request& r, Slot& s);
+    bool admit_one(Request& r, Slot& s, int busy);
     void finish(Slot& s);
     void evict_idle(int64_t need);
     bsj_plan* take_idle(const std::string& shape);
@@ -132,7 +133,11 @@ void bsj_server::evict_idle(int64_t need)
     }
 }
 
-bool bsj_server::admit_one(Request& r, Slot& s)
+namespace bsj {
+bsj_status plan_capture_forms(bsj_plan* p);   // bsj_engine.cu
+}
+
+bool bsj_server::admit_one(Request& r, Slot& s, int busy)
 {
     bsj_instance inst{r.n, r.m, r.machine.data(), r.duration.data()};
     bsj_plan* p = r.prepare ? nullptr : take_idle(r.shape);
@@ -145,7 +150,12 @@ bool bsj_server::admit_one(Request& r, Slot& s)
         evict_idle(r.bytes);
         st = bsj_plan_create(ctx, 1, &inst, 1, &r.beam, &p);
     }
+    // a prepared plan gets the graphs of both selection forms now, off the request path
+    if (st == BSJ_OK && r.prepare) st = bsj::plan_capture_forms(p);
     const Clock::time_point t1 = Clock::now();
+    // the cluster select halves a wide level's latency for about twice the SM time: worth it
+    // while the device has SMs to spare, not when many requests already share it
+    if (st == BSJ_OK) st = bsj_plan_set_select_cluster(p, busy <= cluster_inflight ? 1 : 0);
     if (st == BSJ_OK) st = bsj_plan_run(p, s.stream);
     if (st == BSJ_OK && cudaEventRecord(s.done, s.stream) != cudaSuccess) st = BSJ_ERR_CUDA;
     {
@@ -247,7 +257,7 @@ void bsj_server::run()
                 pending.pop_front();
             }
             r.admitted = Clock::now();
-            if (admit_one(r, s)) {
+            if (admit_one(r, s, busy)) {
                 busy++;
                 std::lock_guard<std::mutex> lk(mu);
                 if (busy > stats.peak_inflight) stats.peak_inflight = busy;
@@ -294,6 +304,15 @@ bsj_status bsj_server_create(bsj_server** out, int device, const bsj_server_conf
         return BSJ_ERR_CUDA;
     }
     s->budget = c.memory_budget > 0 ? c.memory_budget : (int64_t)(free_b / 4 * 3);
+    if (c.cluster_inflight > 0) {
+        s->cluster_inflight = c.cluster_inflight;
+    } else if (c.cluster_inflight == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+        s->cluster_inflight = sms / 8;
+    } else {
+        s->cluster_inflight = -1;
+    }
     s->slots.resize((size_t)c.max_inflight);
     for (Slot& sl : s->slots) {
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -224,6 +224,11 @@ class Plan:
             v |= nat.SELECT[f]
         self.ctx._check(self.lib.bsj_plan_set_select_route(self.h, v))
 
+    def set_select_cluster(self, on: bool):
+        """Cluster select where the rule picks it (True, the default) or one thread block per
+        beam (False) from the next run on (bsj_plan_set_select_cluster); results unchanged."""
+        self.ctx._check(self.lib.bsj_plan_set_select_cluster(self.h, 1 if on else 0))
+
     def select_routes(self) -> set:
         """Names (``_native.ROUTE``) of the selection routes the last run took."""
         r = ctypes.c_uint32()
@@ -265,12 +270,14 @@ class Server:
     ``submit`` queues one solve and returns a ticket at once; the server admits queued
     requests while an in-flight slot and the memory budget allow, runs them concurrently
     and reuses plans by shape.  ``poll`` / ``wait`` return the result dict with
-    ``queue_ms`` and ``run_ms``.  Thread-safe."""
+    ``queue_ms`` and ``run_ms``.  Thread-safe.  ``cluster_inflight``: a request runs the
+    cluster select (K >= 4096) only when at most this many others are in flight at its
+    admission (0 = the device's SMs / 8, negative = never)."""
 
-    def __init__(self, device: int = 0, max_inflight: int = 0, memory_budget: int = 0):
+    def __init__(self, device: int = 0, max_inflight: int = 0, memory_budget: int = 0, cluster_inflight: int = 0):
         self.lib = nat.load()
         h = ctypes.c_void_p()
-        cfg = nat.ServerConfig(int(max_inflight), 0, int(memory_budget))
+        cfg = nat.ServerConfig(int(max_inflight), int(cluster_inflight), int(memory_budget))
         st = self.lib.bsj_server_create(ctypes.byref(h), int(device), ctypes.byref(cfg))
         if st != nat.BSJ_OK:
             raise nat.BsjError(st, "cannot create the server")

@@ -201,6 +201,12 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches
 #define BSJ_ROUTE_CLUSTER  256
 bsj_status bsj_plan_set_select_route(bsj_plan *plan, int32_t flags);
 bsj_status bsj_plan_select_routes(bsj_plan *plan, uint32_t *routes);
+/* enable = 0: one thread block per beam for this plan's selections from its next run on,
+   whatever K (a throughput choice: the cluster form spends about twice the SM time per
+   level for its lower latency); enable != 0 (the default): the cluster form where the
+   rule picks it.  Both forms' graphs are kept, so switching costs one capture per form;
+   the results never depend on it.  The route flags above take precedence. */
+bsj_status bsj_plan_set_select_cluster(bsj_plan *plan, int32_t enable);
 
 /* ---- Autotuning (no counterpart in the reference, whose launch shape is fixed:
    one block of n threads per parent, gpu/v1/solver.cu:186,237) ----
@@ -263,7 +269,9 @@ bsj_status bsj_schedule_decode(const bsj_instance *inst, const int32_t *sequence
 typedef struct bsj_server bsj_server;
 typedef struct {
     int32_t max_inflight;    /* requests on the device at once; 0 = 32, at most 256 */
-    int32_t reserved;
+    int32_t cluster_inflight; /* a request runs the cluster select (K >= 4096) only when at
+                                most this many others are in flight at its admission:
+                                0 = the device's SMs / 8, < 0 = never */
     int64_t memory_budget;   /* device bytes held by running and idle plans; 0 = 3/4 of
                                 the free memory at creation */
 } bsj_server_config;

@@ -142,6 +142,24 @@ def test_cluster_route_default_and_off(ctx, mode):
         assert must <= routes and not (never & routes), what
 
 
+def test_select_cluster_switch(ctx):
+    """bsj_plan_set_select_cluster: one thread block per beam and back, each form's graph
+    kept; the result never changes."""
+    mc, du = synthetic_instance(20, 15, 1)
+    want = O.solve(mc, du, "v2", 4096, 5)
+    plan = ctx.plan([(mc, du)], [BeamSpec("v2", 4096, 500000, 5, 0, -1)])
+    try:
+        for on in (True, False, True, False):
+            plan.set_select_cluster(on)
+            plan.run()
+            got = plan.results()[0]
+            routes = plan.select_routes()
+            _same(got, want, (on, sorted(routes)))
+            assert ("cluster" in routes) == on, (on, sorted(routes))
+    finally:
+        plan.close()
+
+
 def test_route_flags_rejected(ctx):
     mc, du = synthetic_instance(6, 3, 0)
     plan = ctx.plan([(mc, du)], [BeamSpec("v2", 8, 500000, 0, 0, -1)])

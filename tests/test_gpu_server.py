@@ -73,6 +73,23 @@ def test_results_same_alone_and_in_the_mix(ctx):
     assert st["plans_built"] + st["plans_reused"] == len(reqs)
 
 
+@pytest.mark.parametrize("cluster_inflight", [1, -1, 100])
+def test_wide_requests_in_either_select_form(ctx, cluster_inflight):
+    """K=4096 requests: the server gives each the cluster select only while at most
+    cluster_inflight others run (1: some with, some without; -1: never; 100: always).
+    Every result equals the plain solve."""
+    reqs = []
+    for i in range(8):
+        mc, du = synthetic_instance(20, 15, 2000 + i)
+        reqs.append(dict(mc=mc, du=du, mode=("v2", "clean", "v1")[i % 3], K=4096, seed=17 + i))
+    alone = [ctx.solve(r["mc"], r["du"], r["mode"], r["K"], r["seed"]) for r in reqs]
+    with Server(0, max_inflight=4, cluster_inflight=cluster_inflight) as srv:
+        tickets = _submit_from_threads(srv, reqs)
+        got = [srv.wait(t) for t in tickets]
+    for a, g in zip(alone, got):
+        _same(a, g)
+
+
 def test_memory_budget_bounds_what_the_device_holds(ctx):
     reqs = _requests(24, 11)
     sizes = [ctx.estimate([(r["mc"], r["du"])], [_beam(r)]) for r in reqs]
