@@ -70,14 +70,17 @@ constexpr int kSelAll = 511;
 // Routes the levels of a beam took (SegState::select_paths, OR over the levels).
 constexpr uint32_t kPathLarge = 1, kPathDirect = 2, kPathBucket = 4, kPathRadix = 8, kPathDense = 16,
                    kPathRankLsd = 32, kPathRawLsd = 64, kPathBitonic = 128, kPathCluster = 256;
-// CTAs of one beam's cluster select, the smallest beam width it is launched for, and the
-// smallest level (candidate keys) its route takes.  Measured on GB300 (ms per search,
-// cluster / one block): 50x20 K=4096 25.5 / 28.3, 20x15 K=4096 6.97 / 7.37, 100x20 K=4096
-// 69.5 / 100.1; taking only levels above 8 192 keys was slower on every shape, and
-// launching it for K=2048 at 20x15 (levels of ~4.5 K keys) slower than one block.
-constexpr int kSelectCluster = 2;
+// The cluster select: launched for beams of K >= kSelectClusterMinK, its route taken on
+// levels of more than kClusterMinKeys keys, 2 CTAs per beam, or 4 where K * n reaches
+// kSelectClusterWideKN (levels of ~15 K keys and more).  Measured on GB300 (ms per search):
+// one block / 2 CTAs: 50x20 K=4096 28.3 / 25.5, 20x15 K=4096 7.37 / 6.97, 100x20 K=4096
+// 100.1 / 69.5 (taking only levels above 8 192 keys was slower on every shape; launching
+// it for K=2048 at 20x15, levels of ~4.5 K keys, slower than one block); 2 / 4 CTAs:
+// 50x20 K=4096 24.98 / 24.06 (8 beams 27.81 / 27.73), 100x20 K=4096 66.52 / 63.21, 30x20
+// K=4096 13.95 / 14.00, 20x15 K=4096 6.86 / 7.01.
 constexpr int kSelectClusterMinK = 4096;
 constexpr int kClusterMinKeys = 4096;
+constexpr int kSelectClusterWideKN = 150000;
 
 struct SegDesc {
     int32_t n, m, N, K;

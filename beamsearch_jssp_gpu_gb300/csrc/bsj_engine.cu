@@ -72,6 +72,8 @@ struct bsj_plan {
         bool group_ok = false;   // every beam gpu-v2 / clean: the lane-group k_step applies
         int kmax_gpu = 0;        // widest gpu-mode beam (the cluster select is launched from
                                  // kSelectClusterMinK on)
+        int64_t knmax_gpu = 0;   // largest K * n of its gpu-mode beams (4 CTAs per beam from
+                                 // kSelectClusterWideKN on)
     };
     std::vector<Group> groups;
     cudaEvent_t fork = nullptr;
@@ -103,6 +105,7 @@ struct bsj_plan {
     cudaGraphExec_t graph[kNumStepVariants + 1][4] = {};
     bool select_cluster = true;   // bsj_plan_set_select_cluster: the cluster select where the rule picks it
     bool cluster_matters = false; // some beam group is wide enough for the rule to pick it
+    int cluster_beams = 0;        // gpu-mode beams of K >= kSelectClusterMinK (their selects run at once)
     // timing
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -545,7 +548,9 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
                 if (d.mode == BSJ_MODE_V1) gr.has_v1 = true;
                 if (d.mode <= BSJ_MODE_CLEAN) {
                     gr.has_gpu = true;
+                    if (d.K >= kSelectClusterMinK) p->cluster_beams++;
                     gr.kmax_gpu = std::max(gr.kmax_gpu, d.K);
+                    gr.knmax_gpu = std::max(gr.knmax_gpu, (int64_t)d.K * d.n);
                 } else {
                     gr.has_compat = true;
                 }
@@ -563,6 +568,8 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
             p->groups.push_back(gr);
             lo = hi;
         }
+        // too many wide beams for even 2 CTAs each: the select form cannot differ
+        if ((int64_t)p->cluster_beams * 2 > ctx->sm_count) p->cluster_matters = false;
         cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
         for (int g = 0; g < (int)p->groups.size(); g++) cudaEventCreateWithFlags(&p->join[g], cudaEventDisableTiming);
     }
@@ -600,7 +607,13 @@ StepArgs group_args(const bsj_plan* p, const bsj_plan::Group* gr, int v)
     {
         const int fz = p->select_force;
         const bool cl = (fz & kSelForceCluster) || (p->select_cluster && gr && gr->kmax_gpu >= kSelectClusterMinK);
-        a.select_cluster = (cl && !(fz & kSelNoCluster)) ? kSelectCluster : 1;
+        // 4 CTAs per beam for the widest levels, 2 otherwise, and no more CTAs per level than
+        // the device has SMs: a plan running many wide beams at once (a batch) would
+        // otherwise trade its throughput for latency it does not need
+        int csize = (gr && gr->knmax_gpu >= kSelectClusterWideKN) ? 4 : 2;
+        while (csize > 1 && (int64_t)p->cluster_beams * csize > p->ctx->sm_count) csize /= 2;
+        if ((fz & kSelForceCluster) && csize < 2) csize = 2;
+        a.select_cluster = (cl && !(fz & kSelNoCluster) && csize > 1) ? csize : 1;
     }
     a.chunk_prefix = p->d_cprefix + (size_t)ci * (p->nseg + 1);
     a.chunk_lo = p->cprefix[ci][lo];

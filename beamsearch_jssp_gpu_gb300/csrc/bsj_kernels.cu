@@ -3190,7 +3190,9 @@ static cudaError_t set_carveout()
     const int c = cudaSharedmemCarveoutMaxShared;
     cudaError_t e = cudaFuncSetAttribute(k_select, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_select_cl<kSelectCluster>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+        e = cudaFuncSetAttribute(k_select_cl<2>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_select_cl<4>, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_heap, cudaFuncAttributePreferredSharedMemoryCarveout, c);
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int) { return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, c); });
@@ -3221,7 +3223,8 @@ cudaError_t configure_kernels(int sort_cap, const HeapCfg* hc, int sb_max, int m
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = set_carveout();
     if (e == cudaSuccess) e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e == cudaSuccess) e = raise_smem(k_select_cl<kSelectCluster>, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<2>, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<4>, select_smem_bytes(sort_cap));
     if (e == cudaSuccess && hc) e = raise_smem(k_heap, heap_smem_bytes(*hc));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
@@ -3234,7 +3237,8 @@ cudaError_t raise_kernel_smem(int sort_cap, int sb_max, int max_n)
 {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     cudaError_t e = raise_smem(k_select, select_smem_bytes(sort_cap));
-    if (e == cudaSuccess) e = raise_smem(k_select_cl<kSelectCluster>, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<2>, select_smem_bytes(sort_cap));
+    if (e == cudaSuccess) e = raise_smem(k_select_cl<4>, select_smem_bytes(sort_cap));
     if (e == cudaSuccess)
         e = for_each_step([&](auto fn, int ch) { return raise_smem(fn, step_smem_bytes(sb_max, max_n, ch)); });
     if (e == cudaSuccess)
@@ -3313,15 +3317,16 @@ cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t s
     if (a.select_cluster <= 1)
         return launch_kernel(k_select, nseg, kSelectThreads, select_smem_bytes(sort_cap), stream, true, a, s,
                              sort_cap);
-    if (a.select_cluster != kSelectCluster) return cudaErrorInvalidValue;
+    const int C = a.select_cluster;
+    if (C != 2 && C != 4) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)(nseg * kSelectCluster));
+    cfg.gridDim = dim3((unsigned)(nseg * C));
     cfg.blockDim = dim3((unsigned)kSelectThreads);
     cfg.dynamicSmemBytes = select_smem_bytes(sort_cap);
     cfg.stream = stream;
     cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kSelectCluster;
+    at[0].val.clusterDim.x = (unsigned)C;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
@@ -3331,7 +3336,8 @@ cudaError_t launch_select(const StepArgs& a, int s, int sort_cap, cudaStream_t s
         at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.numAttrs = 2;
     }
-    return cudaLaunchKernelEx(&cfg, k_select_cl<kSelectCluster>, a, s, sort_cap);
+    return C == 2 ? cudaLaunchKernelEx(&cfg, k_select_cl<2>, a, s, sort_cap)
+                  : cudaLaunchKernelEx(&cfg, k_select_cl<4>, a, s, sort_cap);
 }
 
 cudaError_t launch_heap(const StepArgs& a, int s, const HeapCfg& hc, cudaStream_t stream)

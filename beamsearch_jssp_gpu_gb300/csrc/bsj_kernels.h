@@ -31,7 +31,7 @@ struct StepArgs {
     int32_t select_force;         // kSel* route flags for k_select (0 = by level size)
     int32_t group_step;           // k_step form: 0 warp per survivor; 1-4 a lane group per
                                   // survivor (k_step_g: 4 lanes copy / bulk, 8 lanes copy / bulk)
-    int32_t select_cluster;       // CTAs per beam of k_select: 1, or kSelectCluster (cluster launch)
+    int32_t select_cluster;       // CTAs per beam of k_select: 1, or 2 / 4 (cluster launch)
     uint8_t* beam_pool;
     uint8_t* slot_pool;
     unsigned long long* keys;

@@ -347,7 +347,7 @@ def gpu_arm(args) -> int:
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_us": 1000.0 * ms / nl,
                 "peak_source": peaks["source"],
-                "regime": "latency-bound: each level of a beam is a dependent chain (select on a 2-SM "
+                "regime": "latency-bound: each level of a beam is a dependent chain (select on a 2- or 4-SM "
                           "cluster, then materialise+expand); the per-level set (~5 MB per beam) stays "
                           "L2-resident, so neither HBM bandwidth nor an SM pipe is saturated",
                 "kernel_share": {k: v[0] / max(1e-9, sum(x[0] for x in kms.values())) for k, v in kms.items()}}

@@ -170,10 +170,10 @@ bsj_status bsj_plan_kernel_ms(const bsj_plan *plan, float *ms, int64_t *launches
    levels onto routes (BSJ_SELECT_* flags OR'd; 0 = the normal choice), so every route
    can be checked on small inputs; the plan's captured graphs are rebuilt on its next
    run.  Beam groups whose widest gpu-mode beam has K >= 4096 run the selection as a
-   cluster of 2 thread blocks per beam, which split the level's keys and exchange only
-   summaries through distributed shared memory (route CLUSTER: the bucket + dense-rank
-   route on both blocks) on levels of more than 8192 candidate keys; smaller levels and
-   those it cannot take fall back to the one-block routes.
+   cluster of 2 thread blocks per beam (4 where K * n >= 150000), which split the level's
+   keys and exchange only summaries through distributed shared memory (route CLUSTER: the
+   bucket + dense-rank route on all blocks) on levels of more than 4096 candidate keys;
+   smaller levels and those it cannot take fall back to the one-block routes.
    BSJ_SELECT_NO_CLUSTER keeps one block per beam, BSJ_SELECT_FORCE_CLUSTER launches the
    cluster form whatever K and takes its route on every level it can (any size).
    BSJ_SELECT_FORCE_LARGE and BSJ_SELECT_NO_LARGE exclude each other, and so do

@@ -13,7 +13,7 @@ synthetic instance of generator seed 0, all in one plan; the same is done here f
   * the oracle (tests/golden/k4096.json "oracle", from tests/golden/gen_k4096.py): the
     makespan, scored children, slots, levels and the SHA-256 of the schedule, in every
     mode.
-At this K the selection runs as a 2-block cluster per beam; gpu-v2 is also checked with
+At this K the selection runs as a cluster of 4 blocks per beam; gpu-v2 is also checked with
 the one-block form (the route flags "no_cluster"), so both are pinned at this size.
 The 8 beams share one bound group (one device best-makespan word, updated by atomicMin),
 as in the measured plan; within a pass every beam prunes against the frozen bound

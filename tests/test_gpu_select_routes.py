@@ -4,9 +4,9 @@ The selection kernel replaces the reference's full stable sort of all child slot
 (cub::DeviceRadixSort::SortPairs, gpu/v1/solver.cu:255-258, gpu/v2_twophases/solver.cu:
 336-339).  By level size it normally takes the direct staged pass or bucket compaction +
 dense-rank sort; the radix-select, raw-LSD, rank-LSD, bitonic and large-level routes run
-only on rare or large levels.  Beams of K >= 4096 run it as a 2-block cluster (the
-bucket + dense-rank route split over both blocks on levels of more than 8 192 keys, the
-one-block routes as its fallback).
+only on rare or large levels.  Beams of K >= 4096 run it as a cluster of 2 blocks (4 where
+K * n >= 150 000): the bucket + dense-rank route split over the blocks on levels of more
+than 4 096 keys, the one-block routes as its fallback.
 bsj_plan_set_select_route forces them onto small levels,
 and each forced search must equal the oracle bit for bit (makespan, schedule, scored
 children, slots, levels) -- where a wrong tie order would show -- and must report that
@@ -140,6 +140,22 @@ def test_cluster_route_default_and_off(ctx, mode):
         what = (mode, flags, sorted(routes))
         _same(got, want, what)
         assert must <= routes and not (never & routes), what
+
+
+@pytest.mark.parametrize("mode", ["v2", "v1"])
+def test_forced_cluster_four_blocks(ctx, mode):
+    """K * n >= 150 000 launches 4 blocks per beam; forced onto every level (down to levels
+    of a few keys, where most blocks hold none), on tie-heavy durations, it equals the
+    oracle."""
+    for mc, du, seed in ((tie_instance(40, 5, 9, 2)[0], tie_instance(40, 5, 9, 2)[1], 3),
+                         (*synthetic_instance(40, 4, 5), 8)):
+        want = O.solve(mc, du, mode, 4096, seed)
+        for flags in (("force_cluster",), ()):
+            got, routes = _run(ctx, mc, du, mode, 4096, seed, flags)
+            what = (mode, flags, sorted(routes))
+            _same(got, want, what)
+            if flags:
+                assert "cluster" in routes, what
 
 
 def test_select_cluster_switch(ctx):
