@@ -243,10 +243,14 @@ int step_var_of_code(int code)
 //  - other groups (v1, ICH/PMS): up to 8 192 survivors per level 8 per CTA, except n > 64
 //    at 4 096 and more, where 32 wins; wider plans 16 per CTA, and 32 where the group alone
 //    holds more than 8 192 or n > 64.
-int rule_chunk_var(int64_t ranks, int nq, int64_t granks, bool group_ok)
+int rule_chunk_var(int64_t ranks, int nq, int64_t granks, bool group_ok, int kmax)
 {
     if (group_ok) {
-        if (nq == 4) return ranks >= 4096 ? step_var_of_code(2) : chunk_var_of(8);
+        // n > 64: the 8-lane bulk form for levels of K >= 2048 survivors (GB300, ms per search:
+        // 100x20 K=4096 1 beam 63.3 -> 53.7, K=2048 8 beams 68.4 -> 57.5, 80x15 K=4096 8 beams
+        // 42.0 -> 37.2 against the 4-lane form), 8 survivors per warp-form CTA below (100x20
+        // K=1024 8 beams: 45.1 against 49.5 for the 8-lane form)
+        if (nq == 4) return kmax >= 2048 ? step_var_of_code(4) : chunk_var_of(8);
         if (ranks <= 2048) return chunk_var_of(8);
         return granks > 8192 ? step_var_of_code(2) : step_var_of_code(3);
     }
@@ -579,7 +583,7 @@ bsj_status plan_build(bsj_context* ctx, int ninst, const bsj_instance* insts, in
         int64_t per_nq[5] = {0, 0, 0, 0, 0};
         for (int b = gr.args.seg_lo; b < gr.args.seg_hi; b++) per_nq[p->segs[b].nq] += p->segs[b].K;
         const int nq = per_nq[4] > per_nq[2] && per_nq[4] > per_nq[1] ? 4 : (per_nq[2] > per_nq[1] ? 2 : 1);
-        gr.rule_var = rule_chunk_var(p->total_ranks, nq, per_nq[1] + per_nq[2] + per_nq[4], gr.group_ok);
+        gr.rule_var = rule_chunk_var(p->total_ranks, nq, per_nq[1] + per_nq[2] + per_nq[4], gr.group_ok, gr.kmax_gpu);
     }
     {
         const int v = tuned_chunk(ctx, p->shape);
