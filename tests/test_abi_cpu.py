@@ -48,6 +48,39 @@ def test_pure_host_calls(lib):
     assert L.bsj_status_string(2).decode().startswith("size")
 
 
+def test_struct_layouts_match_the_compiled_header(tmp_path):
+    """Every public struct's size and member offsets, as a C compiler lays them out from
+    include/bsj.h, equal the ctypes mirrors the Python binding passes to the library."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"bsj_instance": nat.Instance, "bsj_beam": nat.Beam, "bsj_result": nat.Result,
+               "bsj_server_config": nat.ServerConfig, "bsj_request_times": nat.RequestTimes,
+               "bsj_server_stats": nat.ServerStats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "bsj.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["return 0; }"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
 def test_struct_layouts_match_header():
     # bsj_instance: 2 x int32 + 2 pointers; bsj_beam: 6 x 4 B; bsj_result as declared
     assert ctypes.sizeof(nat.Instance) == 8 + 2 * ctypes.sizeof(ctypes.c_void_p)
